@@ -1,0 +1,122 @@
+"""ctypes binding of the in-tree C ABI library (include/gfft_gb300.h).
+
+There is no CPU fallback: when ``libgfft_gb300.so`` is missing the import of
+a compute entry point raises.  ``build()`` compiles it in place.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgfft_gb300.so")
+
+# status codes (include/gfft_gb300.h)
+GFFT_OK = 0
+STATUS_NAMES = {
+    0: "GFFT_OK", 1: "GFFT_E_INVALID_SIZE", 2: "GFFT_E_INVALID_TYPE", 3: "GFFT_E_INVALID_TRANSFORM",
+    4: "GFFT_E_INVALID_PLACE", 5: "GFFT_E_INVALID_DIM", 6: "GFFT_E_INVALID_PARALL", 7: "GFFT_E_NULL_POINTER",
+    8: "GFFT_E_MISALIGNED", 9: "GFFT_E_ALLOC", 10: "GFFT_E_CUDA", 11: "GFFT_E_INVALID_HANDLE",
+    12: "GFFT_E_NOT_IN_LIST", 13: "GFFT_E_TIMEOUT", 14: "GFFT_E_INVALID_PLAN", 15: "GFFT_E_TOO_LARGE",
+}
+
+# every symbol the header declares, checked by the CPU tests
+EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
+            "gfft_get_info", "gfft_plan_query", "gfft_version"]
+
+
+class PlanOpts(ctypes.Structure):
+    _fields_ = [("radix_order", ctypes.c_int), ("max_radix", ctypes.c_int), ("threads_per_block", ctypes.c_int),
+                ("units_per_block", ctypes.c_int), ("max_pass_len", ctypes.c_int),
+                ("kernel_variant", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint64), ("batch", ctypes.c_uint64), ("vtype_id", ctypes.c_int),
+                ("trans_id", ctypes.c_int), ("place_id", ctypes.c_int), ("n_global_passes", ctypes.c_int),
+                ("pass_len", ctypes.c_int * 4), ("radices", (ctypes.c_int * 16) * 4), ("threads", ctypes.c_int * 4),
+                ("units", ctypes.c_int * 4), ("kernel_variant", ctypes.c_int * 4),
+                ("workspace_bytes", ctypes.c_uint64), ("table_bytes", ctypes.c_uint64),
+                ("real_fused", ctypes.c_int), ("kernels_per_exec", ctypes.c_int)]
+
+
+class GfftError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = "%s (%d): %s" % (STATUS_NAMES.get(status, "?"), status, strerror(status) if _lib else "")
+        if what:
+            msg = what + ": " + msg
+        super().__init__(msg)
+
+
+_lib = None
+
+
+def build(force=False):
+    from . import buildlib
+    return buildlib.build(force=force)
+
+
+def lib():
+    """The loaded library; raises if the CUDA extension has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("gfft_gb300 CUDA extension not built (%s missing); run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ci, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64
+        L.gfft_create.argtypes = [ctypes.POINTER(vp), u64, ci, ci, ci, ci, ci, u64]
+        L.gfft_create_opts.argtypes = [ctypes.POINTER(vp), u64, ci, ci, ci, ci, ci, u64, ctypes.POINTER(PlanOpts)]
+        L.gfft_exec.argtypes = [vp, vp, vp, vp]
+        L.gfft_exec_host.argtypes = [vp, vp, vp, vp]
+        L.gfft_destroy.argtypes = [vp]
+        L.gfft_strerror.argtypes = [ci]
+        L.gfft_strerror.restype = ctypes.c_char_p
+        L.gfft_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+        L.gfft_plan_query.argtypes = [u64, ci, ci, ci, u64, ctypes.POINTER(PlanOpts), ctypes.POINTER(PlanInfo)]
+        L.gfft_version.restype = ctypes.c_char_p
+        for name in EXPORTED:
+            getattr(L, name).restype = getattr(L, name).restype or ci
+        L.gfft_strerror.restype = ctypes.c_char_p
+        L.gfft_version.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def info_dict(inf: "PlanInfo") -> dict:
+    d = {f: getattr(inf, f) for f, _ in PlanInfo._fields_}
+    g = inf.n_global_passes
+    d["pass_len"] = list(inf.pass_len)[:g]
+    d["radices"] = [[r for r in inf.radices[i] if r] for i in range(g)]
+    d["threads"] = list(inf.threads)[:g]
+    d["units"] = list(inf.units)[:g]
+    d["kernel_variant"] = list(inf.kernel_variant)[:g]
+    return d
+
+
+def make_opts(opts: dict | None):
+    if not opts:
+        return None
+    o = PlanOpts()
+    for k, v in opts.items():
+        setattr(o, k, int(v))
+    return o
+
+
+def plan_query(n, vtype_id, trans_id, place_id, batch=1, opts=None) -> dict:
+    """Plan without a GPU (gfft_plan_query)."""
+    inf = PlanInfo()
+    o = make_opts(opts)
+    check(lib().gfft_plan_query(n, vtype_id, trans_id, place_id, batch, ctypes.byref(o) if o else None,
+                                ctypes.byref(inf)), "gfft_plan_query")
+    return info_dict(inf)
+
+
+def strerror(status: int) -> str:
+    return lib().gfft_strerror(status).decode()
+
+
+def check(status: int, what: str = ""):
+    if status != GFFT_OK:
+        raise GfftError(status, what)

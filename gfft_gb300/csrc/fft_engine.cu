@@ -1,0 +1,357 @@
+// Batched Stockham FFT engine for sm_103a.
+//
+// One launch = one global pass (see plan.h).  A thread block owns `W` units
+// (whole short transforms, or W adjacent columns of a long one), stages them
+// into shared memory with coalesced loads, runs the in-block radix passes
+// between two padded shared buffers, and writes the result back with
+// coalesced stores.  This replaces the reference's run-time path:
+//   InTimeOOP / InTime recursion      src/gfftalg.h:383-507
+//   DFTk_x_Im_T combine + recurrence  src/gfftalg.h:157-367, src/twiddles.h:212-339
+//   GFFTswap2 digit reversal          src/gfftswap.h:74-227 (not needed: autosort)
+//   Separate (real pre/post pass)     src/gfftswap.h:239-336, fused here
+//   Backward 1/N scaling              src/gfftswap.h:355-374, fused into the store
+//   OpenMP ParallLoop                 src/gfftomp.h:41-189 -> the block grid
+#include <cuda_runtime.h>
+
+#include "butterflies.cuh"
+#include "plan.h"
+
+namespace gfft {
+
+template <typename T> struct PadShift;
+template <> struct PadShift<float> { static constexpr int v = 4; };   // 8-byte elements
+template <> struct PadShift<double> { static constexpr int v = 3; };  // 16-byte elements
+
+template <typename T> __device__ __forceinline__ int pad(int s) { return s + (s >> PadShift<T>::v); }
+
+// one in-block Stockham pass of compile-time radix R over all W units
+template <typename T, int R>
+__device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict__ src,
+                                           typename Vec<T>::t* __restrict__ dst, const EngineArgs& a,
+                                           const BlockPass& p, const typename Vec<T>::t* __restrict__ tw) {
+  typedef typename Vec<T>::t V;
+  const int L = a.L;
+  const int nb = L / R;
+  const int total = a.W * nb;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int lane = i / nb;
+    const int j = i - lane * nb;
+    const V* s = src + lane * a.Lp;
+    V* d = dst + lane * a.Lp;
+    V v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[pad<T>(j + r * nb)];
+    const int k = j % p.Ns;
+    if (p.Ns > 1) {
+      const V* t = tw + p.tw + k;
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(t + (r - 1) * p.Ns));
+    }
+    dft<T, V, R>(v);
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[pad<T>(base + r * p.Ns)] = v[r];
+  }
+}
+
+// generic odd prime radix: every output sums R twiddled inputs (O(R^2))
+template <typename T>
+__device__ void block_pass_generic(const typename Vec<T>::t* __restrict__ src, typename Vec<T>::t* __restrict__ dst,
+                                   const EngineArgs& a, const BlockPass& p, const typename Vec<T>::t* __restrict__ tw) {
+  typedef typename Vec<T>::t V;
+  const int L = a.L, R = p.R;
+  const int nb = L / R;
+  const int total = a.W * L;  // one output per iteration
+  const V* wr = tw + p.gen;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int lane = i / L;
+    const int rem = i - lane * L;
+    const int q = rem / nb;  // output leg
+    const int j = rem - q * nb;
+    const V* s = src + lane * a.Lp;
+    V* d = dst + lane * a.Lp;
+    const int k = j % p.Ns;
+    V acc = mk<V>(0, 0);
+    int m = 0;  // (r*q) mod R
+    for (int r = 0; r < R; ++r) {
+      V x = s[pad<T>(j + r * nb)];
+      if (p.Ns > 1 && r > 0) x = cmul(x, __ldg(tw + p.tw + (r - 1) * p.Ns + k));
+      acc = cadd(acc, cmul(x, __ldg(wr + m)));
+      m += q;
+      if (m >= R) m -= R;
+    }
+    d[pad<T>((j - k) * R + k + q * p.Ns)] = acc;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ typename Vec<T>::t global_twiddle(const EngineArgs& a, long long m) {
+  typedef typename Vec<T>::t V;
+  const V* lo = (const V*)a.gtw_lo;
+  const V* hi = (const V*)a.gtw_hi;
+  const long long q = m / a.gB;
+  return cmul(__ldg(lo + (m - q * a.gB)), __ldg(hi + q));
+}
+
+// global -> shared, with the conjugation of the inverse, the inter-pass
+// twiddle of a multi-pass transform, or the real inverse pre-pass
+template <typename T>
+__device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::t* buf, long long u0) {
+  typedef typename Vec<T>::t V;
+  const V* in = (const V*)a.in;
+  const int L = a.L;
+  const int total = a.W * L;
+  if (a.mode == 0 && a.real == 2) {
+    // real inverse pre pass (the inverse of the reference's Separate with
+    // S=-1, src/gfftswap.h:246-280): X packed -> Z = F + iG
+    const V* rtw = (const V*)a.rtw;
+    const int half = L / 2 + 1;
+    for (int i = threadIdx.x; i < a.W * half; i += blockDim.x) {
+      const int lane = i / half;
+      const int q = i - lane * half;
+      const long long u = u0 + lane;
+      V* b = buf + lane * a.Lp;
+      if (u >= a.nunits) continue;
+      const V* x = in + u * L;
+      if (q == 0) {
+        const V x0 = x[0];  // (X_0, X_n)
+        V z = mk<V>((T)0.5 * (x0.x + x0.y), (T)0.5 * (x0.x - x0.y));
+        b[pad<T>(0)] = cconj(z);
+        continue;
+      }
+      const int qm = L - q;
+      if (q > qm) continue;
+      const V xq = x[q], xm = x[qm];
+      // Z_q = F + i G,  F = (X_q + conj X_m)/2,  G = (X_q - conj X_m) conj(w^q) / 2
+      const V wq = __ldg(rtw + q);
+      V F = mk<V>((T)0.5 * (xq.x + xm.x), (T)0.5 * (xq.y - xm.y));
+      V D = mk<V>((T)0.5 * (xq.x - xm.x), (T)0.5 * (xq.y + xm.y));
+      V G = cmul(D, cconj(wq));
+      V zq = mk<V>(F.x - G.y, F.y + G.x);
+      b[pad<T>(q)] = cconj(zq);
+      if (qm != q) {
+        const V wm = __ldg(rtw + qm);
+        V F2 = mk<V>((T)0.5 * (xm.x + xq.x), (T)0.5 * (xm.y - xq.y));
+        V D2 = mk<V>((T)0.5 * (xm.x - xq.x), (T)0.5 * (xm.y + xq.y));
+        V G2 = cmul(D2, cconj(wm));
+        V zm = mk<V>(F2.x - G2.y, F2.y + G2.x);
+        b[pad<T>(qm)] = cconj(zm);
+      }
+    }
+    return;
+  }
+  if (a.mode == 0) {
+    const V* tile = in + u0 * L;
+    const long long lim = (a.nunits - u0) * L;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int lane = i / L;
+      const int s = i - lane * L;
+      V v = (i < lim) ? tile[i] : mk<V>(0, 0);
+      if (a.conj) v = cconj(v);
+      buf[lane * a.Lp + pad<T>(s)] = v;
+    }
+  } else {
+    const int W = a.W;
+    const long long mstep = a.N / (a.gNs * L);
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int lane = i % W;
+      const int s = i / W;
+      const long long u = u0 + lane;
+      V v = mk<V>(0, 0);
+      if (u < a.nunits) {
+        const long long t = u / a.stride;
+        const long long b = u - t * a.stride;
+        v = in[t * a.N + b + (long long)s * a.stride];
+        if (a.conj) v = cconj(v);
+        if (a.gNs > 1) {
+          const long long k = b % a.gNs;
+          v = cmul(v, global_twiddle<T>(a, (k * s) * mstep));
+        }
+      }
+      buf[lane * a.Lp + pad<T>(s)] = v;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_tile(const EngineArgs& a, const typename Vec<T>::t* buf, long long u0) {
+  typedef typename Vec<T>::t V;
+  V* out = (V*)a.out;
+  const int L = a.L;
+  const int total = a.W * L;
+  const T sc = (T)a.scale;
+  if (a.mode == 0 && a.real == 1) {
+    // real forward post pass (the reference's Separate with S=+1,
+    // src/gfftswap.h:246-280): Z -> X_0, X_n, X_1..X_{n-1}
+    const V* rtw = (const V*)a.rtw;
+    const int half = L / 2 + 1;
+    for (int i = threadIdx.x; i < a.W * half; i += blockDim.x) {
+      const int lane = i / half;
+      const int q = i - lane * half;
+      const long long u = u0 + lane;
+      if (u >= a.nunits) continue;
+      const V* b = buf + lane * a.Lp;
+      V* y = out + u * L;
+      if (q == 0) {
+        const V z0 = b[pad<T>(0)];
+        y[0] = mk<V>(z0.x + z0.y, z0.x - z0.y);
+        continue;
+      }
+      const int qm = L - q;
+      if (q > qm) continue;
+      const V zq = b[pad<T>(q)], zm = b[pad<T>(qm)];
+      {
+        // X_q = F + w^q G, F = (Z_q + conj Z_m)/2, G = -i (Z_q - conj Z_m)/2
+        V F = mk<V>((T)0.5 * (zq.x + zm.x), (T)0.5 * (zq.y - zm.y));
+        V G = mk<V>((T)0.5 * (zq.y + zm.y), (T)-0.5 * (zq.x - zm.x));
+        y[q] = cadd(F, cmul(__ldg(rtw + q), G));
+      }
+      if (qm != q) {
+        V F = mk<V>((T)0.5 * (zm.x + zq.x), (T)0.5 * (zm.y - zq.y));
+        V G = mk<V>((T)0.5 * (zm.y + zq.y), (T)-0.5 * (zm.x - zq.x));
+        y[qm] = cadd(F, cmul(__ldg(rtw + qm), G));
+      }
+    }
+    return;
+  }
+  if (a.mode == 0) {
+    V* tile = out + u0 * L;
+    const long long lim = (a.nunits - u0) * L;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      if (i >= lim) break;
+      const int lane = i / L;
+      const int s = i - lane * L;
+      V v = buf[lane * a.Lp + pad<T>(s)];
+      if (a.conj) v = cconj(v);
+      tile[i] = cscale(v, sc);
+    }
+  } else {
+    const int W = a.W;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int lane = i % W;
+      const int s = i / W;
+      const long long u = u0 + lane;
+      if (u >= a.nunits) continue;
+      const long long t = u / a.stride;
+      const long long b = u - t * a.stride;
+      const long long k = b % a.gNs;
+      V v = buf[lane * a.Lp + pad<T>(s)];
+      if (a.conj) v = cconj(v);
+      out[t * a.N + (b - k) * L + k + (long long)s * a.gNs] = cscale(v, sc);
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) engine_kernel(const __grid_constant__ EngineArgs a) {
+  typedef typename Vec<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* b0 = reinterpret_cast<V*>(smem_raw);
+  V* b1 = b0 + a.W * a.Lp;
+  const long long u0 = (long long)blockIdx.x * a.W;
+  const V* tw = (const V*)a.tw;
+  load_tile<T>(a, b0, u0);
+  __syncthreads();
+  V* src = b0;
+  V* dst = b1;
+  for (int p = 0; p < a.npass; ++p) {
+    const BlockPass bp = a.pass[p];
+    switch (bp.R) {
+      case 16: block_pass<T, 16>(src, dst, a, bp, tw); break;
+      case 8: block_pass<T, 8>(src, dst, a, bp, tw); break;
+      case 4: block_pass<T, 4>(src, dst, a, bp, tw); break;
+      case 2: block_pass<T, 2>(src, dst, a, bp, tw); break;
+      case 3: block_pass<T, 3>(src, dst, a, bp, tw); break;
+      case 5: block_pass<T, 5>(src, dst, a, bp, tw); break;
+      case 7: block_pass<T, 7>(src, dst, a, bp, tw); break;
+      default: block_pass_generic<T>(src, dst, a, bp, tw); break;
+    }
+    __syncthreads();
+    V* t = src;
+    src = dst;
+    dst = t;
+  }
+  store_tile<T>(a, src, u0);
+}
+
+// Real pre/post pass for multi-pass lengths (not fused): in place on
+// `batch` transforms of n complex slots.  dir=1 forward post (Z -> X),
+// dir=2 inverse pre (X -> Z).
+template <typename T>
+__global__ void real_pass_kernel(typename Vec<T>::t* data, long long n, long long batch, int dir,
+                                 const typename Vec<T>::t* __restrict__ rtw) {
+  typedef typename Vec<T>::t V;
+  const long long half = n / 2 + 1;
+  const long long total = half * batch;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long t = i / half;
+    const long long q = i - t * half;
+    V* y = data + t * n;
+    if (q == 0) {
+      const V z0 = y[0];
+      if (dir == 1) y[0] = mk<V>(z0.x + z0.y, z0.x - z0.y);
+      else y[0] = mk<V>((T)0.5 * (z0.x + z0.y), (T)0.5 * (z0.x - z0.y));
+      continue;
+    }
+    const long long qm = n - q;
+    if (q > qm) continue;
+    const V a = y[q], b = y[qm];
+    if (dir == 1) {
+      V F = mk<V>((T)0.5 * (a.x + b.x), (T)0.5 * (a.y - b.y));
+      V G = mk<V>((T)0.5 * (a.y + b.y), (T)-0.5 * (a.x - b.x));
+      V xq = cadd(F, cmul(__ldg(rtw + q), G));
+      V F2 = mk<V>((T)0.5 * (b.x + a.x), (T)0.5 * (b.y - a.y));
+      V G2 = mk<V>((T)0.5 * (b.y + a.y), (T)-0.5 * (b.x - a.x));
+      V xm = cadd(F2, cmul(__ldg(rtw + qm), G2));
+      y[q] = xq;
+      if (qm != q) y[qm] = xm;
+    } else {
+      V F = mk<V>((T)0.5 * (a.x + b.x), (T)0.5 * (a.y - b.y));
+      V D = mk<V>((T)0.5 * (a.x - b.x), (T)0.5 * (a.y + b.y));
+      V G = cmul(D, cconj(__ldg(rtw + q)));
+      V zq = mk<V>(F.x - G.y, F.y + G.x);
+      V F2 = mk<V>((T)0.5 * (b.x + a.x), (T)0.5 * (b.y - a.y));
+      V D2 = mk<V>((T)0.5 * (b.x - a.x), (T)0.5 * (b.y + a.y));
+      V G2 = cmul(D2, cconj(__ldg(rtw + qm)));
+      V zm = mk<V>(F2.x - G2.y, F2.y + G2.x);
+      y[q] = zq;
+      if (qm != q) y[qm] = zm;
+    }
+  }
+}
+
+}  // namespace gfft
+
+// host-side launchers (called from gfft_capi.cpp)
+extern "C" int gfft_engine_setup(int dbl, size_t max_smem) {
+  cudaError_t e;
+  if (dbl)
+    e = cudaFuncSetAttribute(gfft::engine_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  else
+    e = cudaFuncSetAttribute(gfft::engine_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
+extern "C" int gfft_engine_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                  cudaStream_t stream) {
+  if (dbl) gfft::engine_kernel<double><<<grid, threads, smem, stream>>>(*a);
+  else gfft::engine_kernel<float><<<grid, threads, smem, stream>>>(*a);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
+                                     cudaStream_t stream) {
+  long long total = (n / 2 + 1) * batch;
+  unsigned threads = 256;
+  long long blocks = (total + threads - 1) / threads;
+  if (blocks > 152LL * 16) blocks = 152LL * 16;
+  if (blocks < 1) blocks = 1;
+  if (dbl)
+    gfft::real_pass_kernel<double><<<(unsigned)blocks, threads, 0, stream>>>((double2*)data, n, batch, dir,
+                                                                            (const double2*)rtw);
+  else
+    gfft::real_pass_kernel<float><<<(unsigned)blocks, threads, 0, stream>>>((float2*)data, n, batch, dir,
+                                                                          (const float2*)rtw);
+  return (int)cudaGetLastError();
+}

@@ -1,0 +1,378 @@
+// C ABI of the library (declared in include/gfft_gb300.h).
+//
+// A handle is the GPU counterpart of one reference transform object
+// (GFFT::Transform<...>::Instance, src/gfftgen.h:46-87): it owns the plan,
+// the device twiddle tables (the reference keeps "no additional data",
+// release_notes.txt:55, and recomputes twiddles per call) and the workspace
+// of a multi-pass transform.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/gfft_gb300.h"
+#include "plan.h"
+
+extern "C" int gfft_engine_setup(int dbl, size_t max_smem);
+extern "C" int gfft_engine_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                  cudaStream_t stream);
+extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
+                                     cudaStream_t stream);
+
+struct gfft_plan {
+  HostPlan hp;
+  int vtype = 0;
+  int device = 0;
+  void* d_tab = nullptr;
+  size_t tab_bytes = 0;
+  void* d_ws[2] = {nullptr, nullptr};
+  size_t ws_bytes = 0;
+  // staging buffers for gfft_exec_host, allocated on first use
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
+  unsigned magic = 0x6FF7B300u;
+};
+
+namespace {
+
+const unsigned kMagic = 0x6FF7B300u;
+
+bool valid(gfft_handle h) { return h && h->magic == kMagic; }
+
+int setup_device_once(int dbl) {
+  static std::mutex mu;
+  static bool done[2][64] = {{false}};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GFFT_E_CUDA;
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 64 && done[dbl][dev]) return GFFT_OK;
+  int maxopt = 0;
+  cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (gfft_engine_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
+  if (dev < 64) done[dbl][dev] = true;
+  return GFFT_OK;
+}
+
+size_t elem_bytes(int dbl) { return dbl ? 16 : 8; }
+
+int parse_opts(const gfft_plan_opts* opts, PlanOpts& po) {
+  if (!opts) return GFFT_OK;
+  if (opts->max_radix && opts->max_radix != 2 && opts->max_radix != 4 && opts->max_radix != 8 &&
+      opts->max_radix != 16)
+    return GFFT_E_INVALID_PLAN;
+  if (opts->threads_per_block &&
+      (opts->threads_per_block < 32 || opts->threads_per_block > 512 || opts->threads_per_block % 32))
+    return GFFT_E_INVALID_PLAN;
+  if (opts->units_per_block < 0 || opts->max_pass_len < 0 || opts->radix_order < 0 || opts->radix_order > 2)
+    return GFFT_E_INVALID_PLAN;
+  po.radix_order = opts->radix_order;
+  po.max_radix = opts->max_radix ? opts->max_radix : 16;
+  po.threads = opts->threads_per_block;
+  po.units = opts->units_per_block;
+  po.max_pass_len = opts->max_pass_len;
+  po.variant = opts->kernel_variant;
+  return GFFT_OK;
+}
+
+int check_ids(uint64_t n, int vtype_id, int trans_id, int dim, int parall_id, int place_id, uint64_t batch) {
+  if (vtype_id < 0 || vtype_id > 3) return GFFT_E_INVALID_TYPE;
+  if (trans_id < 0 || trans_id > 3) return GFFT_E_INVALID_TRANSFORM;
+  if (place_id < 0 || place_id > 1) return GFFT_E_INVALID_PLACE;
+  if (dim != 1) return GFFT_E_INVALID_DIM;
+  if (parall_id < 0) return GFFT_E_INVALID_PARALL;
+  if (n == 0 || batch == 0 || n > (1ULL << 40) || batch > (1ULL << 40)) return GFFT_E_INVALID_SIZE;
+  return GFFT_OK;
+}
+
+void fill_info(const HostPlan& p, int vtype, size_t tab_bytes, size_t ws_bytes, gfft_plan_info* info) {
+  std::memset(info, 0, sizeof(*info));
+  info->n = (uint64_t)p.n;
+  info->batch = (uint64_t)p.batch;
+  info->vtype_id = vtype;
+  info->trans_id = p.trans;
+  info->place_id = p.place;
+  info->n_global_passes = p.nglobal;
+  for (int g = 0; g < p.nglobal && g < 4; ++g) {
+    info->pass_len[g] = p.gp[g].L;
+    for (int i = 0; i < p.gp[g].npass && i < 15; ++i) info->radices[g][i] = p.gp[g].pass[i].R;
+    info->threads[g] = p.gp[g].threads;
+    info->units[g] = p.gp[g].units;
+    info->kernel_variant[g] = p.gp[g].variant;
+  }
+  info->workspace_bytes = (uint64_t)ws_bytes * (uint64_t)p.n_ws;
+  info->table_bytes = (uint64_t)tab_bytes;
+  info->real_fused = p.real_fused;
+  info->kernels_per_exec = p.nglobal + ((p.trans >= 2 && !p.real_fused) ? 1 : 0);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gfft_version(void) { return "gfft_gb300 0.1 (sm_103a)"; }
+
+const char* gfft_strerror(int status) {
+  switch (status) {
+    case GFFT_OK: return "success";
+    case GFFT_E_INVALID_SIZE: return "invalid transform length or batch";
+    case GFFT_E_INVALID_TYPE: return "invalid value type id";
+    case GFFT_E_INVALID_TRANSFORM: return "invalid transform type id";
+    case GFFT_E_INVALID_PLACE: return "invalid place id (in place requires src == dst)";
+    case GFFT_E_INVALID_DIM: return "only one-dimensional transforms are implemented";
+    case GFFT_E_INVALID_PARALL: return "invalid parallelization id";
+    case GFFT_E_NULL_POINTER: return "null pointer";
+    case GFFT_E_MISALIGNED: return "pointer not aligned to a complex element";
+    case GFFT_E_ALLOC: return "memory allocation failed";
+    case GFFT_E_CUDA: return "CUDA runtime error";
+    case GFFT_E_INVALID_HANDLE: return "invalid handle";
+    case GFFT_E_NOT_IN_LIST:
+      return "Requested transform is not compiled! Check your instantiation of GenerateTransform class!";
+    case GFFT_E_TIMEOUT: return "a bounded device wait timed out";
+    case GFFT_E_INVALID_PLAN: return "inconsistent plan options";
+    case GFFT_E_TOO_LARGE: return "request exceeds the fixed capacity of this entry point";
+    default: return "unknown status";
+  }
+}
+
+int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim, int parall_id,
+                     int place_id, uint64_t batch, const gfft_plan_opts* opts) {
+  if (!handle) return GFFT_E_NULL_POINTER;
+  *handle = nullptr;
+  int st0 = check_ids(n, vtype_id, trans_id, dim, parall_id, place_id, batch);
+  if (st0 != GFFT_OK) return st0;
+  PlanOpts po;
+  st0 = parse_opts(opts, po);
+  if (st0 != GFFT_OK) return st0;
+  const int dbl = (vtype_id == 0 || vtype_id == 2) ? 1 : 0;
+  gfft_plan* h = new (std::nothrow) gfft_plan();
+  if (!h) return GFFT_E_ALLOC;
+  if (gfft_plan_build(h->hp, (long long)n, (long long)batch, dbl, trans_id, place_id, po) != 0) {
+    delete h;
+    return GFFT_E_INVALID_SIZE;
+  }
+  h->vtype = vtype_id;
+  int st = setup_device_once(dbl);
+  if (st != GFFT_OK) {
+    delete h;
+    return st;
+  }
+  cudaGetDevice(&h->device);
+  int maxopt = 0;
+  cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  for (int g = 0; g < h->hp.nglobal; ++g)
+    if (h->hp.gp[g].smem > (size_t)maxopt) {
+      delete h;
+      return GFFT_E_INVALID_SIZE;
+    }
+  // tables: generated in extended precision, rounded once to the working type
+  const size_t cnt = std::max<size_t>(h->hp.table_count, 1);
+  std::vector<double> tab(2 * cnt, 0.0);
+  gfft_plan_tables(h->hp, tab.data());
+  h->tab_bytes = cnt * elem_bytes(dbl);
+  if (cudaMalloc(&h->d_tab, h->tab_bytes) != cudaSuccess) {
+    delete h;
+    return GFFT_E_ALLOC;
+  }
+  cudaError_t ce;
+  if (dbl) {
+    ce = cudaMemcpy(h->d_tab, tab.data(), h->tab_bytes, cudaMemcpyHostToDevice);
+  } else {
+    std::vector<float> f(2 * cnt);
+    for (size_t i = 0; i < 2 * cnt; ++i) f[i] = (float)tab[i];
+    ce = cudaMemcpy(h->d_tab, f.data(), h->tab_bytes, cudaMemcpyHostToDevice);
+  }
+  if (ce != cudaSuccess) {
+    cudaFree(h->d_tab);
+    delete h;
+    return GFFT_E_CUDA;
+  }
+  if (h->hp.n_ws > 0) {
+    h->ws_bytes = h->hp.ws_elems * elem_bytes(dbl);
+    for (int i = 0; i < h->hp.n_ws; ++i)
+      if (cudaMalloc(&h->d_ws[i], h->ws_bytes) != cudaSuccess) {
+        for (int j = 0; j < i; ++j) cudaFree(h->d_ws[j]);
+        cudaFree(h->d_tab);
+        delete h;
+        return GFFT_E_ALLOC;
+      }
+  }
+  *handle = h;
+  return GFFT_OK;
+}
+
+int gfft_create(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim, int parall_id, int place_id,
+                uint64_t batch) {
+  return gfft_create_opts(handle, n, vtype_id, trans_id, dim, parall_id, place_id, batch, nullptr);
+}
+
+int gfft_destroy(gfft_handle h) {
+  if (!valid(h)) return GFFT_E_INVALID_HANDLE;
+  h->magic = 0;
+  cudaFree(h->d_tab);
+  for (int i = 0; i < 2; ++i)
+    if (h->d_ws[i]) cudaFree(h->d_ws[i]);
+  if (h->d_stage) cudaFree(h->d_stage);
+  delete h;
+  return GFFT_OK;
+}
+
+int gfft_get_info(gfft_handle h, gfft_plan_info* info) {
+  if (!valid(h)) return GFFT_E_INVALID_HANDLE;
+  if (!info) return GFFT_E_NULL_POINTER;
+  fill_info(h->hp, h->vtype, h->tab_bytes, h->ws_bytes, info);
+  return GFFT_OK;
+}
+
+int gfft_plan_query(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch, const gfft_plan_opts* opts,
+                    gfft_plan_info* info) {
+  if (!info) return GFFT_E_NULL_POINTER;
+  int st = check_ids(n, vtype_id, trans_id, 1, 0, place_id, batch);
+  if (st != GFFT_OK) return st;
+  PlanOpts po;
+  st = parse_opts(opts, po);
+  if (st != GFFT_OK) return st;
+  HostPlan hp;
+  const int dbl = (vtype_id == 0 || vtype_id == 2) ? 1 : 0;
+  if (gfft_plan_build(hp, (long long)n, (long long)batch, dbl, trans_id, place_id, po) != 0)
+    return GFFT_E_INVALID_SIZE;
+  const size_t esz = elem_bytes(dbl);
+  fill_info(hp, vtype_id, std::max<size_t>(hp.table_count, 1) * esz, hp.ws_elems * esz, info);
+  return GFFT_OK;
+}
+
+// shared by gfft_exec and the scratch-free entry point: runs the plan with
+// the given workspace buffers
+int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream, void* ws0, void* ws1) {
+  const HostPlan& p = h->hp;
+  const int dbl = p.dbl;
+  const size_t esz = elem_bytes(dbl);
+  const char* tab = (const char*)h->d_tab;
+  const bool inverse = (p.trans == 1 || p.trans == 3);
+  const long long n = p.n, batch = p.batch;
+  const void* cur_in = src;
+  // real inverse with several passes: unfused pre pass in place on dst
+  if (p.trans == 3 && !p.real_fused) {
+    if (dst != src) {
+      if (cudaMemcpyAsync(dst, src, (size_t)n * batch * esz, cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+        return GFFT_E_CUDA;
+    }
+    if (gfft_real_pass_launch(dbl, dst, n, batch, 2, tab + p.rtw_off * esz, stream) != 0) return GFFT_E_CUDA;
+    cur_in = dst;
+  }
+  // buffer sequence of the global passes
+  std::vector<const void*> ins(p.nglobal);
+  std::vector<void*> outs(p.nglobal);
+  const bool inplace = (cur_in == dst);
+  if (p.nglobal == 1) {
+    ins[0] = cur_in;
+    outs[0] = dst;
+  } else if (p.nglobal % 2 == 0) {
+    // in -> ws -> dst -> ws -> dst
+    const void* a = cur_in;
+    for (int g = 0; g < p.nglobal; ++g) {
+      ins[g] = a;
+      outs[g] = (g % 2 == 0) ? ws0 : dst;
+      a = outs[g];
+    }
+  } else if (!inplace) {
+    // in -> dst -> ws -> dst (-> ws -> dst)
+    const void* a = cur_in;
+    for (int g = 0; g < p.nglobal; ++g) {
+      ins[g] = a;
+      outs[g] = (g % 2 == 0) ? dst : ws0;
+      a = outs[g];
+    }
+  } else {
+    // in place, odd: in -> ws0 -> ws1 -> dst (the second buffer of an
+    // out-of-place plan called in place is allocated on first need)
+    if (!ws1 && ws0 == h->d_ws[0]) {
+      if (cudaMalloc(&h->d_ws[1], h->ws_bytes) != cudaSuccess) {
+        h->d_ws[1] = nullptr;
+        return GFFT_E_ALLOC;
+      }
+      ws1 = h->d_ws[1];
+    }
+    if (!ws1) return GFFT_E_INVALID_PLAN;
+    ins[0] = cur_in;
+    outs[0] = ws0;
+    ins[1] = ws0;
+    outs[1] = ws1;
+    ins[2] = ws1;
+    outs[2] = dst;
+  }
+  for (int g = 0; g < p.nglobal; ++g) {
+    const GlobalPass& gp = p.gp[g];
+    EngineArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.in = ins[g];
+    a.out = outs[g];
+    a.N = n;
+    a.L = gp.L;
+    a.stride = n / gp.L;
+    a.nunits = batch * a.stride;
+    a.gNs = gp.Ns;
+    a.gB = (long long)p.gtw_B;
+    a.gtw_lo = tab + p.gtw_lo_off * esz;
+    a.gtw_hi = tab + p.gtw_hi_off * esz;
+    a.tw = tab;
+    a.rtw = tab + p.rtw_off * esz;
+    a.pad_shift = dbl ? 3 : 4;
+    a.Lp = gp.L + (gp.L >> a.pad_shift) + 1;
+    a.W = gp.units;
+    a.mode = gp.mode;
+    a.npass = gp.npass;
+    for (int i = 0; i < gp.npass; ++i) a.pass[i] = gp.pass[i];
+    const bool last = (g == p.nglobal - 1);
+    a.real = p.real_fused ? ((p.trans == 2) ? 1 : 2) : 0;
+    // The inverse runs as conj(FFT(conj x)) / N.  Every pass conjugates on
+    // load and on store: the pairs cancel between passes, so the inter-pass
+    // twiddles see forward-domain data.  The fused real inverse pre pass
+    // conjugates inside its own load.
+    a.conj = inverse ? 1 : 0;
+    a.scale = (inverse && last) ? 1.0 / (double)n : 1.0;
+    long long grid = (a.nunits + a.W - 1) / a.W;
+    if (grid > 0x7FFFFFFFLL) return GFFT_E_INVALID_SIZE;
+    if (gfft_engine_launch(dbl, &a, (unsigned)grid, (unsigned)gp.threads, gp.smem, stream) != 0)
+      return GFFT_E_CUDA;
+  }
+  if (p.trans == 2 && !p.real_fused) {
+    if (gfft_real_pass_launch(dbl, dst, n, batch, 1, tab + p.rtw_off * esz, stream) != 0) return GFFT_E_CUDA;
+  }
+  return GFFT_OK;
+}
+
+int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
+  if (!valid(h)) return GFFT_E_INVALID_HANDLE;
+  if (!src || !dst) return GFFT_E_NULL_POINTER;
+  const size_t al = h->hp.dbl ? 16 : 8;
+  if (((uintptr_t)src % al) || ((uintptr_t)dst % al)) return GFFT_E_MISALIGNED;
+  if (h->hp.place == 0 && src != dst) return GFFT_E_INVALID_PLACE;
+  return gfft_exec_ws(h, src, dst, (cudaStream_t)stream, h->d_ws[0], h->d_ws[1]);
+}
+
+int gfft_exec_host(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
+  if (!valid(h)) return GFFT_E_INVALID_HANDLE;
+  if (!src || !dst) return GFFT_E_NULL_POINTER;
+  if (h->hp.place == 0 && src != dst) return GFFT_E_INVALID_PLACE;
+  const size_t bytes = (size_t)h->hp.n * (size_t)h->hp.batch * elem_bytes(h->hp.dbl);
+  if (!h->d_stage) {
+    if (cudaMalloc(&h->d_stage, bytes) != cudaSuccess) {
+      h->d_stage = nullptr;
+      return GFFT_E_ALLOC;
+    }
+    h->stage_bytes = bytes;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(h->d_stage, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return GFFT_E_CUDA;
+  int st = gfft_exec_ws(h, h->d_stage, h->d_stage, s, h->d_ws[0], h->d_ws[1]);
+  if (st != GFFT_OK) return st;
+  if (cudaMemcpyAsync(dst, h->d_stage, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return GFFT_E_CUDA;
+  return GFFT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,99 @@
+// Internal plan structures shared by the host planner (planner.cpp) and the
+// CUDA kernels (fft_engine.cu).
+//
+// A transform of length N (complex points) runs as 1..4 "global passes".
+// Global pass g is one Stockham step with super-radix L_g over the whole
+// array (Stockham autosort: natural-order output, no digit-reversal pass,
+// which replaces the reference's GFFTswap2, src/gfftswap.h:74-227):
+//
+//   for each unit (t, b), t < batch, b < N/L_g, k = b mod Ns_g:
+//     v[r]  = x[t*N + b + r*(N/L_g)] * W_{Ns_g*L_g}^{k*r}      r < L_g
+//     v     = DFT_{L_g}(v)                                       (in one block)
+//     y[t*N + (b/Ns_g)*Ns_g*L_g + k + r*Ns_g] = v[r]
+//
+// with Ns_g = L_0*...*L_{g-1}.  One thread block computes DFT_{L_g} for
+// `units` consecutive units in shared memory, as a sequence of in-block
+// Stockham passes of radix R in {2,3,4,5,7,8,16} (or a generic odd prime).
+#pragma once
+#include <cstdint>
+
+#define GFFT_MAXP 16     // in-block passes
+#define GFFT_MAXG 4      // global passes
+
+struct BlockPass {
+  int R;    // radix
+  int Ns;   // product of the radices before this pass
+  int tw;   // offset (complex elements) of this pass's twiddles in the table
+  int gen;  // generic odd prime: offset of its W_R^m table (else -1)
+};
+
+// Arguments of one launch of the engine kernel (passed by value).
+struct EngineArgs {
+  const void* in;
+  void* out;
+  long long nunits;   // batch * (N / L)
+  long long N;        // transform length
+  long long stride;   // N / L
+  long long gNs;      // Ns of this global pass
+  long long gB;       // global twiddle split: W_N^m = lo[m % gB] * hi[m / gB]
+  const void* gtw_lo;
+  const void* gtw_hi;
+  const void* tw;     // in-block pass twiddles (+ generic prime tables)
+  const void* rtw;    // real pre/post twiddles W_{2n}^q, q < n
+  int L;              // in-block length
+  int Lp;             // padded per-unit stride in shared memory
+  int W;              // units per block
+  int mode;           // 0: units are whole contiguous transforms; 1: lane units
+  int npass;
+  int conj;           // inverse transform as conj(FFT(conj(x)))
+  int real;           // 0 none, 1 real forward post pass, 2 real inverse pre pass
+  int pad_shift;      // shared-memory padding: one slot per 2^pad_shift elements
+  double scale;       // output scale
+  BlockPass pass[GFFT_MAXP];
+};
+
+struct GlobalPass {
+  int L;
+  long long Ns;
+  int units;      // W
+  int threads;
+  int mode;
+  int variant;    // 1 generic engine, 2 register-resident fast path
+  int npass;
+  BlockPass pass[GFFT_MAXP];
+  size_t smem;
+};
+
+struct PlanOpts {
+  int radix_order = 0;
+  int max_radix = 16;
+  int threads = 0;
+  int units = 0;
+  int max_pass_len = 0;
+  int variant = 0;
+};
+
+struct HostPlan {
+  long long n = 0;        // complex length of the transform
+  long long batch = 1;
+  int dbl = 0;            // 1 = FP64, 0 = FP32
+  int trans = 0;          // 0 DFT, 1 IDFT, 2 RDFT, 3 IRDFT
+  int place = 1;
+  int nglobal = 0;
+  GlobalPass gp[GFFT_MAXG];
+  int real_fused = 0;     // real pre/post pass inside the single global pass
+  // host copy of the device tables (FP64 values; converted at upload)
+  std::size_t tw_count = 0;      // in-block twiddles (complex)
+  std::size_t gtw_lo_off = 0, gtw_hi_off = 0, gtw_B = 1;
+  std::size_t rtw_off = 0;
+  std::size_t table_count = 0;   // total complex entries
+  std::size_t ws_elems = 0;      // workspace, complex elements
+  int n_ws = 0;                  // number of workspace buffers (0..2)
+};
+
+// planner.cpp
+int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int trans, int place,
+                    const PlanOpts& opts);
+// Fill `tab` (2*table_count doubles, interleaved) with every table the plan
+// references, generated in extended precision and rounded once.
+void gfft_plan_tables(const HostPlan& plan, double* tab);

@@ -1,0 +1,277 @@
+// Host planner: the run-time replacement for the reference's compile-time
+// factorisation and twiddle generation.
+//
+//  - The reference factorises N at compile time into ascending primes
+//    (Factorize, src/gfftfactor.h:160-169) and recurses one prime per level
+//    (InTimeOOP, src/gfftalg.h:459-507).  Here N is split into 1..4 global
+//    passes ("super-radices" that fit one thread block) and each of those into
+//    in-block Stockham radices {16, 8, 4, 2, 7, 5, 3} plus a generic odd
+//    prime, so a power of two uses radix 16 instead of radix 2.
+//  - The reference computes the first root of each level from compile-time
+//    decimal series (GetFirstRoot, src/metaroot.h:104-120) and every other
+//    twiddle by a run-time complex recurrence (ComputeRoots,
+//    src/twiddles.h:234-339; radix 2 in the working type, src/gfftalg.h:
+//    249-265).  Here every twiddle is computed directly in extended precision
+//    with exact integer angle reduction and rounded once to the working type,
+//    so there is no recurrence error.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "plan.h"
+
+namespace {
+
+struct PF {
+  long long p;
+  int k;
+};
+
+std::vector<PF> factorize(long long n) {
+  std::vector<PF> f;
+  for (long long p = 2; p * p <= n; p += (p == 2 ? 1 : 2)) {
+    int k = 0;
+    while (n % p == 0) {
+      n /= p;
+      ++k;
+    }
+    if (k) f.push_back({p, k});
+  }
+  if (n > 1) f.push_back({n, 1});
+  return f;
+}
+
+// cos and sin of 2*pi*j/m in long double, j reduced exactly and folded into
+// the first octant before the library call.
+void root(long long j, long long m, long double* c, long double* s) {
+  j %= m;
+  if (j < 0) j += m;
+  const long double PI4 = 0.785398163397448309615660845819875721L;
+  // angle = 2*pi*j/m = (8j/m) * pi/4
+  __int128 e = (__int128)8 * j;
+  long long oct = (long long)(e / m);
+  long long r = (long long)(e - (__int128)oct * m);
+  bool flip = oct & 1;
+  long double a = flip ? (long double)(m - r) / (long double)m * PI4 : (long double)r / (long double)m * PI4;
+  long double ca = cosl(a), sa = sinl(a), cc, ss;
+  switch (oct) {
+    case 0: cc = ca; ss = sa; break;
+    case 1: cc = sa; ss = ca; break;
+    case 2: cc = -sa; ss = ca; break;
+    case 3: cc = -ca; ss = sa; break;
+    case 4: cc = -ca; ss = -sa; break;
+    case 5: cc = -sa; ss = -ca; break;
+    case 6: cc = sa; ss = -ca; break;
+    default: cc = ca; ss = -sa; break;
+  }
+  *c = cc;
+  *s = ss;
+}
+
+// forward root W_m^j = exp(-2 pi i j / m)
+void wroot(long long j, long long m, double* re, double* im) {
+  long double c, s;
+  root(j, m, &c, &s);
+  *re = (double)c;
+  *im = (double)(-s);
+}
+
+std::vector<int> block_radices(int L, const PlanOpts& o) {
+  std::vector<int> pow2, odd, gen;
+  int a = 0;
+  int m = L;
+  while (m % 2 == 0) {
+    m /= 2;
+    ++a;
+  }
+  int mr = o.max_radix;
+  int lg = mr >= 16 ? 4 : mr >= 8 ? 3 : mr >= 4 ? 2 : 1;
+  int q = a / lg, rem = a % lg;
+  for (int i = 0; i < q; ++i) pow2.push_back(1 << lg);
+  if (rem) {
+    if (lg == 4 && rem == 1 && q >= 1) {
+      pow2.pop_back();
+      pow2.push_back(8);
+      pow2.push_back(4);
+    } else {
+      pow2.push_back(1 << rem);
+    }
+  }
+  for (long long p : {7LL, 5LL, 3LL}) {
+    while (m % p == 0) {
+      m /= (int)p;
+      odd.push_back((int)p);
+    }
+  }
+  for (const PF& f : factorize(m))
+    for (int i = 0; i < f.k; ++i) gen.push_back((int)f.p);
+  std::vector<int> seq;
+  if (o.radix_order == 2) {
+    seq.insert(seq.end(), gen.begin(), gen.end());
+    seq.insert(seq.end(), odd.begin(), odd.end());
+    seq.insert(seq.end(), pow2.begin(), pow2.end());
+  } else {
+    seq.insert(seq.end(), pow2.begin(), pow2.end());
+    seq.insert(seq.end(), odd.begin(), odd.end());
+    seq.insert(seq.end(), gen.begin(), gen.end());
+    if (o.radix_order == 1) std::reverse(seq.begin(), seq.end());
+  }
+  return seq;
+}
+
+// split N into `P` factors, each <= cap, balanced in log; false if impossible
+bool split_passes(long long N, int P, long long cap, std::vector<long long>& out) {
+  std::vector<long long> primes;
+  for (const PF& f : factorize(N))
+    for (int i = 0; i < f.k; ++i) primes.push_back(f.p);
+  std::sort(primes.rbegin(), primes.rend());
+  std::vector<long long> g(P, 1);
+  for (long long p : primes) {
+    int best = -1;
+    for (int i = 0; i < P; ++i)
+      if (g[i] * p <= cap && (best < 0 || g[i] < g[best])) best = i;
+    if (best < 0) return false;
+    g[best] *= p;
+  }
+  std::sort(g.rbegin(), g.rend());
+  out = g;
+  return true;
+}
+
+int round32(long long x) { return (int)std::max<long long>(32, (x + 31) / 32 * 32); }
+
+}  // namespace
+
+int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int trans, int place,
+                    const PlanOpts& opts) {
+  if (n < 1 || batch < 1) return 1;
+  plan = HostPlan();
+  plan.n = n;
+  plan.batch = batch;
+  plan.dbl = dbl;
+  plan.trans = trans;
+  plan.place = place;
+  PlanOpts o = opts;
+  if (o.max_radix <= 0) o.max_radix = 16;
+
+  const int esz = dbl ? 16 : 8;
+  const int pad_shift = dbl ? 3 : 4;
+  const long long smem_budget = 160 * 1024;
+  auto padded = [&](long long L) { return L + (L >> pad_shift) + 1; };
+  // largest single-pass length: two padded buffers of one transform
+  long long cap1 = dbl ? 4096 : 8192;
+  if (o.max_pass_len > 0) cap1 = std::min<long long>(cap1, o.max_pass_len);
+  const int lane_w = o.units > 0 ? o.units : (dbl ? 4 : 8);  // 64-byte rows
+  long long capL = 1;
+  while (2 * lane_w * padded(capL * 2) * esz <= smem_budget) capL *= 2;
+  if (o.max_pass_len > 0) capL = std::min<long long>(capL, o.max_pass_len);
+
+  std::vector<long long> Ls;
+  if (n <= cap1) {
+    Ls.push_back(n);
+  } else {
+    bool ok = false;
+    for (int P = 2; P <= GFFT_MAXG && !ok; ++P) ok = split_passes(n, P, capL, Ls);
+    if (!ok) return 1;  // a prime factor larger than one block can hold
+  }
+  plan.nglobal = (int)Ls.size();
+  std::size_t tw = 0;
+  long long Ns = 1;
+  for (int g = 0; g < plan.nglobal; ++g) {
+    GlobalPass& gp = plan.gp[g];
+    gp.L = (int)Ls[g];
+    gp.Ns = Ns;
+    gp.mode = plan.nglobal == 1 ? 0 : 1;
+    std::vector<int> rs = block_radices(gp.L, o);
+    if ((int)rs.size() > GFFT_MAXP) return 1;
+    gp.npass = (int)rs.size();
+    int bNs = 1;
+    int rmin = 16;
+    for (int i = 0; i < gp.npass; ++i) {
+      BlockPass& bp = gp.pass[i];
+      bp.R = rs[i];
+      bp.Ns = bNs;
+      bp.tw = (int)tw;
+      bp.gen = -1;
+      tw += (std::size_t)(bp.R - 1) * bNs;
+      bNs *= bp.R;
+      rmin = std::min(rmin, bp.R);
+    }
+    for (int i = 0; i < gp.npass; ++i) {
+      BlockPass& bp = gp.pass[i];
+      if (bp.R > 16 || (bp.R != 2 && bp.R != 3 && bp.R != 4 && bp.R != 5 && bp.R != 7 && bp.R != 8 &&
+                        bp.R != 16)) {
+        bp.gen = (int)tw;
+        tw += bp.R;
+      }
+    }
+    if (gp.mode == 0) {
+      long long target = dbl ? 2048 : 4096;  // elements per block
+      int W = o.units > 0 ? o.units : (int)std::max<long long>(1, target / gp.L);
+      W = (int)std::min<long long>(W, batch);
+      while (W > 1 && 2LL * W * padded(gp.L) * esz > smem_budget) --W;
+      gp.units = W;
+    } else {
+      long long stride = n / gp.L;
+      gp.units = (int)std::min<long long>(lane_w, stride);
+    }
+    long long elems = (long long)gp.units * gp.L;
+    int thr = o.threads > 0 ? o.threads : round32(std::min<long long>(512, std::max<long long>(64, elems / 16)));
+    gp.threads = thr;
+    gp.variant = 1;
+    gp.smem = (size_t)(2LL * gp.units * padded(gp.L) * esz);
+    Ns *= gp.L;
+  }
+  plan.tw_count = tw;
+  // global four-step twiddles W_N^m = lo[m % B] * hi[m / B]
+  std::size_t off = tw;
+  if (plan.nglobal > 1) {
+    long long B = 1;
+    while (B * B < n) B *= 2;
+    plan.gtw_B = (std::size_t)B;
+    plan.gtw_lo_off = off;
+    off += (std::size_t)B;
+    plan.gtw_hi_off = off;
+    off += (std::size_t)((n + B - 1) / B);
+  }
+  if (trans >= 2) {
+    plan.rtw_off = off;
+    off += (std::size_t)n;
+    plan.real_fused = plan.nglobal == 1 ? 1 : 0;
+  }
+  plan.table_count = off;
+  // workspace: odd pass counts in place need two buffers
+  if (plan.nglobal >= 2) {
+    plan.ws_elems = (std::size_t)(n * batch);
+    plan.n_ws = (plan.nglobal % 2 == 1 && place == 0) ? 2 : 1;
+  }
+  return 0;
+}
+
+void gfft_plan_tables(const HostPlan& plan, double* tab) {
+  for (int g = 0; g < plan.nglobal; ++g) {
+    const GlobalPass& gp = plan.gp[g];
+    for (int i = 0; i < gp.npass; ++i) {
+      const BlockPass& bp = gp.pass[i];
+      const long long M = (long long)bp.Ns * bp.R;
+      for (int r = 1; r < bp.R; ++r)
+        for (int k = 0; k < bp.Ns; ++k) {
+          std::size_t e = (std::size_t)bp.tw + (std::size_t)(r - 1) * bp.Ns + k;
+          wroot((long long)k * r, M, &tab[2 * e], &tab[2 * e + 1]);
+        }
+      if (bp.gen >= 0)
+        for (int m = 0; m < bp.R; ++m) wroot(m, bp.R, &tab[2 * (bp.gen + m)], &tab[2 * (bp.gen + m) + 1]);
+    }
+  }
+  if (plan.nglobal > 1) {
+    const long long B = (long long)plan.gtw_B;
+    for (long long m = 0; m < B; ++m)
+      wroot(m, plan.n, &tab[2 * (plan.gtw_lo_off + m)], &tab[2 * (plan.gtw_lo_off + m) + 1]);
+    for (long long q = 0; q < (plan.n + B - 1) / B; ++q)
+      wroot(q * B, plan.n, &tab[2 * (plan.gtw_hi_off + q)], &tab[2 * (plan.gtw_hi_off + q) + 1]);
+  }
+  if (plan.trans >= 2)
+    for (long long q = 0; q < plan.n; ++q)
+      wroot(q, 2 * plan.n, &tab[2 * (plan.rtw_off + q)], &tab[2 * (plan.rtw_off + q) + 1]);
+}

@@ -1,0 +1,135 @@
+/*
+ * gfft_gb300 — C ABI of the GB300 (sm_103a) implementation of GFFT's
+ * transform hot path.
+ *
+ * The reference (scpp/gfft) is a header-only C++ template library with no C
+ * ABI: a transform object is made by GFFT::GenerateTransform<...> and looked
+ * up by CreateTransformObject(n, vtype_id, trans_id, dim, parall_id,
+ * place_id) (src/gfftgen.h:189-231); its fft(T*) / fft(const T*, T*)
+ * virtual call (src/gfftpolicy.h:46-58) runs the transform.  The entry points
+ * below are what a foreign-function binding of that path needs: plain
+ * integers, sizes and pointers, a status code instead of a C++ exception.
+ *
+ * Conventions (identical to the reference):
+ *   - data is interleaved (re, im), contiguous; a COMPLEX_* value type has
+ *     the same bytes as the matching real one (std::complex<T>);
+ *   - DFT  (trans_id 0) computes X_k = sum_n x_n e^{-2 pi i k n / N};
+ *     IDFT (trans_id 1) uses e^{+2 pi i k n / N} and scales by 1/N
+ *     (src/gfftspec.h:117-135, src/gfftswap.h:338-374);
+ *   - RDFT (trans_id 2) of length n transforms 2n reals into the packed
+ *     half spectrum X_0, X_n, X_1 .. X_{n-1}; IRDFT (3) inverts it,
+ *     IRDFT(RDFT(x)) = x (src/gfftswap.h:239-287, src/gfftpolicy.h:262-297);
+ *   - value type IDs DOUBLE=0, FLOAT=1, COMPLEX_DOUBLE=2, COMPLEX_FLOAT=3;
+ *     place IDs IN_PLACE=0, OUT_OF_PLACE=1; parallel IDs Serial=0,
+ *     OpenMP<NT>=NT-1 (src/gfftpolicy.h:78-453).  Every parallel ID maps to
+ *     the same batched GPU grid.
+ *
+ * Beyond the reference: a batch count, in-place composite N, out-of-place and
+ * non-power-of-two real transforms, and device-resident execution on a CUDA
+ * stream.  Handles are immutable after creation and own their device
+ * twiddle tables and workspace; calls on one handle must be serialised on one
+ * stream (they share the workspace).
+ */
+#ifndef GFFT_GB300_H
+#define GFFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gfft_plan* gfft_handle;
+typedef struct CUstream_st* gfft_stream; /* a cudaStream_t; NULL = legacy default stream */
+
+/* status codes */
+enum {
+  GFFT_OK = 0,
+  GFFT_E_INVALID_SIZE = 1,      /* n == 0, batch == 0, or a length this build cannot plan */
+  GFFT_E_INVALID_TYPE = 2,      /* vtype_id not in {0,1,2,3} */
+  GFFT_E_INVALID_TRANSFORM = 3, /* trans_id not in {0,1,2,3} */
+  GFFT_E_INVALID_PLACE = 4,     /* place_id not in {0,1}, or in place with src != dst */
+  GFFT_E_INVALID_DIM = 5,       /* dim != 1 */
+  GFFT_E_INVALID_PARALL = 6,    /* parall_id < 0 */
+  GFFT_E_NULL_POINTER = 7,
+  GFFT_E_MISALIGNED = 8,        /* pointer not aligned to one complex element */
+  GFFT_E_ALLOC = 9,             /* device or host allocation failed */
+  GFFT_E_CUDA = 10,             /* a CUDA runtime call or launch failed */
+  GFFT_E_INVALID_HANDLE = 11,
+  GFFT_E_NOT_IN_LIST = 12,      /* size/type not generated by the facade's typelist */
+  GFFT_E_TIMEOUT = 13,          /* a bounded device wait ran out (persistent kernels) */
+  GFFT_E_INVALID_PLAN = 14,     /* a caller-supplied plan option is inconsistent */
+  GFFT_E_TOO_LARGE = 15         /* request exceeds a fixed capacity of the entry point */
+};
+
+/* Replaces GenerateTransform<...>::CreateTransformObject(n, vtype_id,
+ * trans_id, dim, parall_id, place_id) (src/gfftgen.h:222-231) plus the
+ * Transform::Create() it ends in (src/gfftgen.h:81-83).  `n` is the transform
+ * length (complex points; for RDFT/IRDFT the complex length of the packed
+ * 2n reals).  `batch` transforms lie back to back (stride 2n scalars). */
+int gfft_create(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim, int parall_id,
+                int place_id, uint64_t batch);
+
+/* Plan options (the autotuner's knobs).  Zero means "planner default". */
+typedef struct gfft_plan_opts {
+  int radix_order;        /* 0 = default order, 1 = reversed, 2 = odd radices first */
+  int max_radix;          /* largest in-block radix: 16, 8, 4 or 2 (0 = 16) */
+  int threads_per_block;  /* 32..512, multiple of 32 */
+  int units_per_block;    /* transforms (single-pass) or lanes (multi-pass) per block */
+  int max_pass_len;       /* cap on one pass's in-block length (forces more passes) */
+  int kernel_variant;     /* 0 = auto, 1 = generic engine, 2 = register-resident fast path */
+  int reserved[6];
+} gfft_plan_opts;
+
+int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim,
+                     int parall_id, int place_id, uint64_t batch, const gfft_plan_opts* opts);
+
+/* Replaces AbstractFFT_inp<T>::fft(T*) and AbstractFFT_oop<T>::fft(const T*,
+ * T*) (src/gfftpolicy.h:46-58) for DEVICE pointers: in place when
+ * src == dst.  Asynchronous on `stream`. */
+int gfft_exec(gfft_handle handle, const void* src, void* dst, gfft_stream stream);
+
+/* The same call on HOST pointers (what the reference's fft() receives):
+ * copies in, transforms, copies out on `stream` and waits for it. */
+int gfft_exec_host(gfft_handle handle, const void* src, void* dst, gfft_stream stream);
+
+/* Replaces `delete obj` of the object Create() returned (src/gfftgen.h:81-83). */
+int gfft_destroy(gfft_handle handle);
+
+/* Text of a status code (replaces TransformFactoryError::Exception::what(),
+ * src/gfftgen.h:133-145, for GFFT_E_NOT_IN_LIST). */
+const char* gfft_strerror(int status);
+
+/* Plan description, for logs and the autotuner (no reference counterpart:
+ * the reference's plan is its compile-time factor list, src/gfftfactor.h). */
+typedef struct gfft_plan_info {
+  uint64_t n, batch;
+  int vtype_id, trans_id, place_id;
+  int n_global_passes;         /* HBM round trips of the complex transform */
+  int pass_len[4];             /* in-block length of each global pass */
+  int radices[4][16];          /* in-block radix sequence of each pass (0-terminated) */
+  int threads[4], units[4];    /* launch shape of each pass */
+  int kernel_variant[4];       /* 1 generic engine, 2 register-resident fast path */
+  uint64_t workspace_bytes;    /* device scratch owned by the handle */
+  uint64_t table_bytes;        /* device twiddle tables owned by the handle */
+  int real_fused;              /* real pre/post pass fused into the transform */
+  int kernels_per_exec;        /* kernel launches of one gfft_exec */
+} gfft_plan_info;
+
+int gfft_get_info(gfft_handle handle, gfft_plan_info* info);
+
+/* Plan a transform without creating it (no GPU needed): fills `info` as
+ * gfft_get_info would for the same arguments.  No reference counterpart
+ * (the reference plans at compile time). */
+int gfft_plan_query(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
+                    const gfft_plan_opts* opts, gfft_plan_info* info);
+
+/* Library version string. */
+const char* gfft_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFFT_GB300_H */

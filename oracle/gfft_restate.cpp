@@ -216,6 +216,25 @@ static void odd_core(long_t K, const OddConsts<T>& oc, T x0r, T x0i, const T* sr
   (void)sizeof(LT);
 }
 
+/* per-butterfly temporaries: on the stack for primes up to 129 */
+template <class T>
+struct Scratch {
+  T fixed[4 * 64];
+  std::vector<T> heap;
+  T *sr, *si, *dr, *di;
+  explicit Scratch(long_t H) {
+    T* b = fixed;
+    if (H > 64) {
+      heap.resize(4 * H);
+      b = heap.data();
+    }
+    sr = b;
+    si = b + H;
+    dr = b + 2 * H;
+    di = b + 3 * H;
+  }
+};
+
 /* In-place butterfly on legs data[0], data[M2], ..., data[(K-1)*M2]
  * (DFTk_inp<K,M2>), untwiddled. */
 template <class T>
@@ -251,7 +270,8 @@ struct InpButterfly {
       data[I21] = ti + dif_r;
     } else {
       const long_t H = (K - 1) / 2, NM = K * M;
-      std::vector<T> sr(H), si(H), dr(H), di(H);
+      Scratch<T> sc(H);
+      T *sr = sc.sr, *si = sc.si, *dr = sc.dr, *di = sc.di;
       for (long_t i = 0; i < H; ++i) {
         const long_t k = (i + 1) * M;
         sr[i] = data[k] + data[NM - k];
@@ -259,7 +279,7 @@ struct InpButterfly {
         dr[i] = data[k] - data[NM - k];
         di[i] = data[k + 1] - data[NM - k + 1];
       }
-      transform_odd(data, M, sr.data(), si.data(), dr.data(), di.data());
+      transform_odd(data, M, sr, si, dr, di);
     }
   }
 
@@ -313,7 +333,8 @@ struct InpButterfly {
       return;
     }
     const long_t H = (K - 1) / 2, NM = K * M;
-    std::vector<T> sr(H), si(H), dr(H), di(H);
+    Scratch<T> sc(H);
+    T *sr = sc.sr, *si = sc.si, *dr = sc.dr, *di = sc.di;
     for (long_t i = 0; i < H; ++i) {
       const long_t k = (i + 1) * M;
       const T tr1 = data[k] * wr[i] - data[k + 1] * wi[i];
@@ -325,13 +346,13 @@ struct InpButterfly {
       dr[i] = tr1 - tr2;
       di[i] = ti1 - ti2;
     }
-    transform_odd(data, M, sr.data(), si.data(), dr.data(), di.data());
+    transform_odd(data, M, sr, si, dr, di);
   }
 };
 
 /* Out-of-place leaf DFTk<K,SI,DI> (src/gfftspec.h:42-188) */
 template <class T>
-static void leaf_oop(long_t K, int S, const T* src, long_t SI, T* dst, long_t DI) {
+static void leaf_oop(long_t K, int S, const InpButterfly<T>& bf, const T* src, long_t SI, T* dst, long_t DI) {
   if (K == 2) {
     const T tr = src[0] - src[SI];
     const T ti = src[1] - src[SI + 1];
@@ -340,7 +361,7 @@ static void leaf_oop(long_t K, int S, const T* src, long_t SI, T* dst, long_t DI
     dst[DI] = tr;
     dst[DI + 1] = ti;
   } else if (K == 3) {
-    const T m_coef = coef3<T>(S);
+    const T m_coef = bf.m_coef;
     const long_t SI2 = SI + SI, DI2 = DI + DI;
     const T sr = src[SI] + src[SI2];
     const T dr = m_coef * (src[SI] - src[SI2]);
@@ -355,9 +376,10 @@ static void leaf_oop(long_t K, int S, const T* src, long_t SI, T* dst, long_t DI
     dst[DI2] = tr - di;
     dst[DI2 + 1] = ti + dr;
   } else {
-    OddConsts<T> oc(K, S);
+    const OddConsts<T>& oc = bf.oc;
     const long_t H = (K - 1) / 2, NSI = K * SI;
-    std::vector<T> sr(H), si(H), dr(H), di(H);
+    Scratch<T> sc(H);
+    T *sr = sc.sr, *si = sc.si, *dr = sc.dr, *di = sc.di;
     for (long_t i = 0; i < H; ++i) {
       const long_t k = (i + 1) * SI;
       sr[i] = src[k] + src[NSI - k];
@@ -365,7 +387,7 @@ static void leaf_oop(long_t K, int S, const T* src, long_t SI, T* dst, long_t DI
       dr[i] = src[k] - src[NSI - k];
       di[i] = src[k + 1] - src[NSI - k + 1];
     }
-    odd_core<T>(K, oc, src[0], src[1], sr.data(), si.data(), dr.data(), di.data(), dst, DI);
+    odd_core<T>(K, oc, src[0], src[1], sr, si, dr, di, dst, DI);
     dst[0] = src[0];
     dst[1] = src[1];
     for (long_t i = 0; i < H; ++i) {
@@ -378,9 +400,8 @@ static void leaf_oop(long_t K, int S, const T* src, long_t SI, T* dst, long_t DI
 /* Combine pass DFTk_x_Im_T<K, ., M, Step=1> on data of K*M complex values
  * with first root W1 of length K*M. */
 template <class T>
-static void combine(long_t K, long_t M, int S, const Root<T>& W1, T* data) {
+static void combine(long_t K, long_t M, const InpButterfly<T>& bf, const Root<T>& W1, T* data) {
   typedef typename VType<T>::LT LT;
-  InpButterfly<T> bf(K, S);
   const long_t M2 = 2 * M; /* leg stride in scalars */
   if (K == 2) {
     if (M == 2) { /* SimpleSpec == 2 (src/gfftalg.h:355-367) */
@@ -411,7 +432,14 @@ static void combine(long_t K, long_t M, int S, const Root<T>& W1, T* data) {
   }
   /* general: ComputeRoots<K> in TempType (src/twiddles.h:291-339) */
   bf.apply(data, M2);
-  std::vector<LT> wpr(K - 1), wpi(K - 1), wr(K - 1), wi(K - 1);
+  LT fixed[4 * 32];
+  std::vector<LT> heap;
+  LT* b = fixed;
+  if (K - 1 > 32) {
+    heap.resize(4 * (K - 1));
+    b = heap.data();
+  }
+  LT *wpr = b, *wpi = b + (K - 1), *wr = b + 2 * (K - 1), *wi = b + 3 * (K - 1);
   wpr[0] = W1.re;
   wpi[0] = W1.im;
   for (long_t i = 0; i < K - 2; ++i) {
@@ -422,14 +450,14 @@ static void combine(long_t K, long_t M, int S, const Root<T>& W1, T* data) {
     wr[i] = wpr[i];
     wi[i] = wpi[i];
   }
-  bf.apply_tw(data + 2, M2, wr.data(), wi.data());
+  bf.apply_tw(data + 2, M2, wr, wi);
   for (long_t j = 4; j < M2; j += 2) {
     for (long_t i = 0; i < K - 1; ++i) { /* RootsContainer::step */
       LT tt = wr[i];
       wr[i] = tt * wpr[i] - wi[i] * wpi[i];
       wi[i] = wi[i] * wpr[i] + tt * wpi[i];
     }
-    bf.apply_tw(data + j, M2, wr.data(), wi.data());
+    bf.apply_tw(data + j, M2, wr, wi);
   }
 }
 
@@ -451,35 +479,63 @@ static std::vector<Factor> factorize(long_t n) {
   return f;
 }
 
-/* InTimeOOP (src/gfftalg.h:459-507): `fl` is the remaining factor list */
+/* Everything a transform object holds constant between calls: the prime
+ * peeled at each recursion depth, each depth's root, one butterfly object per
+ * prime (the reference keeps these in its compile-time types and objects). */
 template <class T>
-static void intime_oop(long_t N, std::vector<Factor> fl, int S, long_t LastK, const T* src, T* dst,
-                       int depth, const RootTable* rt) {
-  while (!fl.empty() && fl[0].k == 0) fl.erase(fl.begin());
-  const long_t K = fl[0].p;
+struct Ctx {
+  int S;
+  std::vector<long_t> level;  /* prime peeled at depth d (ascending order) */
+  std::vector<Root<T> > root; /* first root of the length at depth d */
+  std::vector<InpButterfly<T>*> bf_of_depth;
+  std::vector<InpButterfly<T>*> own;
+  Ctx(long_t n, int S_, const RootTable* rt) : S(S_) {
+    for (const Factor& f : factorize(n))
+      for (long_t i = 0; i < f.k; ++i) level.push_back(f.p);
+    long_t N = n;
+    for (size_t d = 0; d < level.size(); ++d) {
+      root.push_back(level_root<T>(N, S, (int)d, rt));
+      InpButterfly<T>* b = nullptr;
+      for (InpButterfly<T>* o : own)
+        if (o->K == level[d]) b = o;
+      if (!b) {
+        b = new InpButterfly<T>(level[d], S);
+        own.push_back(b);
+      }
+      bf_of_depth.push_back(b);
+      N /= level[d];
+    }
+  }
+  ~Ctx() {
+    for (InpButterfly<T>* o : own) delete o;
+  }
+};
+
+/* InTimeOOP (src/gfftalg.h:459-507) */
+template <class T>
+static void intime_oop(long_t N, const Ctx<T>& c, long_t LastK, const T* src, T* dst, int depth) {
+  const long_t K = c.level[depth];
   if (N == K) { /* prime leaf */
-    leaf_oop<T>(K, S, src, 2 * LastK, dst, 2);
+    leaf_oop<T>(K, c.S, *c.bf_of_depth[depth], src, 2 * LastK, dst, 2);
     return;
   }
   const long_t M = N / K;
-  std::vector<Factor> next = fl;
-  next[0].k -= 1;
   for (long_t m = 0, lk = 0; m < 2 * N; m += 2 * M, lk += 2 * LastK)
-    intime_oop<T>(M, next, S, K * LastK, src + lk, dst + m, depth + 1, rt);
-  combine<T>(K, M, S, level_root<T>(N, S, depth, rt), dst);
+    intime_oop<T>(M, c, K * LastK, src + lk, dst + m, depth + 1);
+  combine<T>(K, M, *c.bf_of_depth[depth], c.root[depth], dst);
 }
 
 /* InTime (src/gfftalg.h:400-442), after the digit reversal; prime powers */
 template <class T>
-static void intime_inp(long_t N, long_t p, int S, T* data, int depth, const RootTable* rt) {
+static void intime_inp(long_t N, const Ctx<T>& c, T* data, int depth) {
+  const long_t p = c.level[depth];
   if (N == p) {
-    InpButterfly<T> bf(p, S);
-    bf.apply(data, 2);
+    c.bf_of_depth[depth]->apply(data, 2);
     return;
   }
   const long_t M = N / p;
-  for (long_t m = 0; m < 2 * N; m += 2 * M) intime_inp<T>(M, p, S, data + m, depth + 1, rt);
-  combine<T>(p, M, S, level_root<T>(N, S, depth, rt), data);
+  for (long_t m = 0; m < 2 * N; m += 2 * M) intime_inp<T>(M, c, data + m, depth + 1);
+  combine<T>(p, M, *c.bf_of_depth[depth], c.root[depth], data);
 }
 
 /* base-p digit reversal of N = p^P complex values (GFFTswap2) */
@@ -556,9 +612,16 @@ enum { OK = 0, E_SIZE = 1, E_PLACE = 2, E_TYPE = 3 };
 /* One transform object of the reference: trans 0=DFT 1=IDFT 2=RDFT 3=IRDFT,
  * place 0=IN_PLACE 1=OUT_OF_PLACE.  Returns a status. */
 template <class T>
-static int exec_one(long_t n, int trans, int place, const T* src, T* dst, const RootTable* rt) {
+static int exec_one(long_t n, int trans, int place, const T* src, T* dst, const RootTable* rt,
+                    const Ctx<T>* cx = nullptr) {
   if (n < 1) return E_SIZE;
   const int S = (trans == 0 || trans == 2) ? 1 : -1;
+  Ctx<T>* own = nullptr;
+  if (!cx && n > 1) cx = own = new Ctx<T>(n, S, rt);
+  struct Del {
+    Ctx<T>* p;
+    ~Del() { delete p; }
+  } del_{own};
   if (trans >= 2) {
     /* real transforms: in place, N a power of two (src/gfftswap.h:282-286) */
     long_t p;
@@ -569,7 +632,7 @@ static int exec_one(long_t n, int trans, int place, const T* src, T* dst, const 
     if (trans == 3) separate<T>(n, S, d);
     if (n > 1) {
       digit_reverse<T>(n, 2, d);
-      intime_inp<T>(n, 2, S, d, 0, rt);
+      intime_inp<T>(n, *cx, d, 0);
     }
     if (trans == 3) backward<T>(n, d);
     if (trans == 2) separate<T>(n, S, d);
@@ -584,17 +647,35 @@ static int exec_one(long_t n, int trans, int place, const T* src, T* dst, const 
     if (!is_prime_power(n, &p)) return E_PLACE;
     if (dst != src) std::memcpy(dst, src, sizeof(T) * 2 * n);
     digit_reverse<T>(n, p, dst);
-    intime_inp<T>(n, p, S, dst, 0, rt);
+    intime_inp<T>(n, *cx, dst, 0);
   } else {
     if (n == 1) {
       dst[0] = src[0];
       dst[1] = src[1];
     } else {
-      intime_oop<T>(n, factorize(n), S, 1, src, dst, 0, rt);
+      intime_oop<T>(n, *cx, 1, src, dst, 0);
     }
   }
   if (trans == 1) backward<T>(n, dst);
   return OK;
+}
+
+template <class T>
+static int exec_batch(int64_t n, int64_t batch, int trans, int place, const T* src, T* dst, int nthreads) {
+  const int S = (trans == 0 || trans == 2) ? 1 : -1;
+  Ctx<T> cx(n > 1 ? n : 2, S, nullptr);
+  int err = 0;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads) reduction(max : err)
+#endif
+  for (int64_t b = 0; b < batch; ++b) {
+    int e = exec_one<T>(n, trans, place, src + (size_t)b * 2 * n, dst + (size_t)b * 2 * n, nullptr,
+                        n > 1 ? &cx : nullptr);
+    if (e > err) err = e;
+  }
+  (void)nthreads;
+  return err;
 }
 
 }  // namespace
@@ -617,24 +698,14 @@ int orc_gfft_exec_roots(int64_t n, int vtype, int trans, int place, const void* 
   return E_TYPE;
 }
 
-/* Batched: transform b reads src + b*2n scalars and writes dst + b*2n.
- * nthreads <= 0 uses every OpenMP thread.  Returns the first error. */
+/* Batched: transform b reads src + b*2n scalars and writes dst + b*2n;
+ * one context (roots, butterfly constants) shared by the whole batch, an
+ * OpenMP loop over the batch.  nthreads <= 0 uses every OpenMP thread. */
 int orc_gfft_exec_batch(int64_t n, int64_t batch, int vtype, int trans, int place, const void* src,
                         void* dst, int nthreads) {
-  const size_t esz = vtype == 0 ? sizeof(double) : sizeof(float);
-  int err = 0;
-#ifdef _OPENMP
-  if (nthreads <= 0) nthreads = omp_get_max_threads();
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(max : err)
-#endif
-  for (int64_t b = 0; b < batch; ++b) {
-    const char* s = (const char*)src + (size_t)b * 2 * n * esz;
-    char* d = (char*)dst + (size_t)b * 2 * n * esz;
-    int e = orc_gfft_exec(n, vtype, trans, place, s, d);
-    if (e > err) err = e;
-  }
-  (void)nthreads;
-  return err;
+  if (vtype == 0) return exec_batch<double>(n, batch, trans, place, (const double*)src, (double*)dst, nthreads);
+  if (vtype == 1) return exec_batch<float>(n, batch, trans, place, (const float*)src, (float*)dst, nthreads);
+  return E_TYPE;
 }
 
 int orc_num_threads(void) {

@@ -1,0 +1,127 @@
+"""CPU: the C-ABI library builds, loads and exports every declared symbol;
+host logic (planner, option validation, facade errors) without a GPU."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+import gfft_gb300
+from gfft_gb300 import _lib
+from gfft_gb300 import gfft as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    syms = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        if "extern \"C\"" not in text and "extern \"C\" {" not in text:
+            continue
+        for m in re.finditer(r"^\s*(?:const\s+)?[\w\s\*]+?\b(gfft_\w+)\s*\(", text, re.M):
+            syms.add(m.group(1))
+    return syms
+
+
+def test_build_and_load():
+    path = gfft_gb300.build()
+    assert os.path.exists(path)
+    L = _lib.lib()
+    assert L.gfft_version().decode().startswith("gfft_gb300")
+
+
+def test_exports_every_declared_symbol():
+    L = _lib.lib()
+    declared = _declared_symbols()
+    assert {"gfft_create", "gfft_exec", "gfft_destroy", "gfft_strerror"} <= declared
+    for s in declared:
+        assert hasattr(L, s), s
+    assert set(_lib.EXPORTED) <= declared
+
+
+def test_strerror():
+    assert _lib.strerror(0) == "success"
+    assert _lib.strerror(12) == ("Requested transform is not compiled! Check your instantiation of "
+                                 "GenerateTransform class!")
+    assert _lib.strerror(999) == "unknown status"
+
+
+@pytest.mark.parametrize("n,vt,passes", [(1, 0, 1), (2, 1, 1), (1024, 0, 1), (4096, 1, 1), (8192, 1, 1),
+                                         (8192, 0, 2), (786432, 0, 2), (390625, 1, 2), (248832, 0, 2),
+                                         (1 << 24, 1, 3), (1 << 27, 1, 3)])
+def test_plan_shapes(n, vt, passes):
+    d = _lib.plan_query(n, vt, 0, 1, 1)
+    assert d["n_global_passes"] == passes
+    prod = 1
+    for L, rs in zip(d["pass_len"], d["radices"]):
+        p = 1
+        for r in rs:
+            p *= r
+        assert p == L
+        prod *= L
+    assert prod == n
+    if passes > 1:
+        assert d["workspace_bytes"] == n * (16 if vt in (0, 2) else 8)
+
+
+def test_plan_power_of_two_uses_radix16():
+    d = _lib.plan_query(4096, 1, 0, 1, 65536)
+    assert d["radices"] == [[16, 16, 16]]
+    d = _lib.plan_query(4096, 1, 0, 1, 1, {"max_radix": 4})
+    assert d["radices"] == [[4] * 6]
+
+
+def test_plan_errors():
+    with pytest.raises(_lib.GfftError) as e:
+        _lib.plan_query(0, 0, 0, 1)
+    assert e.value.status == 1
+    with pytest.raises(_lib.GfftError) as e:
+        _lib.plan_query(16, 7, 0, 1)
+    assert e.value.status == 2
+    with pytest.raises(_lib.GfftError) as e:
+        _lib.plan_query(16, 0, 9, 1)
+    assert e.value.status == 3
+    with pytest.raises(_lib.GfftError) as e:
+        _lib.plan_query(16, 0, 0, 3)
+    assert e.value.status == 4
+    with pytest.raises(_lib.GfftError) as e:
+        _lib.plan_query(16, 0, 0, 1, 1, {"max_radix": 6})
+    assert e.value.status == 14
+    # a prime factor larger than one block holds cannot be planned
+    with pytest.raises(_lib.GfftError) as e:
+        _lib.plan_query(2 * 4099, 1, 0, 1)
+    assert e.value.status == 1
+
+
+def test_real_plans():
+    d = _lib.plan_query(1 << 19, 0, 2, 0, 16)
+    assert d["real_fused"] == 0 and d["kernels_per_exec"] == d["n_global_passes"] + 1
+    d = _lib.plan_query(2048, 0, 2, 0, 16)
+    assert d["real_fused"] == 1 and d["kernels_per_exec"] == 1
+
+
+def test_tags_and_ids():
+    assert (G.DOUBLE.ID, G.FLOAT.ID, G.COMPLEX_DOUBLE.ID, G.COMPLEX_FLOAT.ID) == (0, 1, 2, 3)
+    assert (G.DFT.ID, G.IDFT.ID, G.RDFT.ID, G.IRDFT.ID) == (0, 1, 2, 3)
+    assert (G.IN_PLACE.ID, G.OUT_OF_PLACE.ID) == (0, 1)
+    assert G.Serial.ID == 0 and G.OpenMP(4).ID == 3 and G.OpenMP(1) is G.Serial
+    assert G.DFT.Inverse is G.IDFT and G.RDFT.Inverse is G.IRDFT
+    assert G.PlaceGroup.Default is G.OUT_OF_PLACE and G.TransformTypeGroup.Default is G.DFT
+
+
+def test_factory_unknown_combination_raises():
+    ts = G.GenerateTransform([16, 32], G.DOUBLE, [G.DFT, G.IDFT], 1, G.Serial, G.OUT_OF_PLACE)
+    assert len(ts.Result) == 4
+    for bad in [dict(n=64, vtype_id=0), dict(n=16, vtype_id=1), dict(n=16, vtype_id=0, trans_id=2),
+                dict(n=16, vtype_id=0, parall_id=3), dict(n=16, vtype_id=0, place_id=0),
+                dict(n=16, vtype_id=0, dim=2)]:
+        with pytest.raises(G.TransformFactoryError.Exception) as e:
+            ts.CreateTransformObject(**bad)
+        assert e.value.what() == ("Requested transform is not compiled! Check your instantiation of "
+                                  "GenerateTransform class!")
+
+
+def test_plan_opts_layout():
+    assert ctypes.sizeof(_lib.PlanOpts) == 12 * 4

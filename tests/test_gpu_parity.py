@@ -1,0 +1,349 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+Tolerances (relative L2 error against the exact oracle, binary128 DFT or
+long-double FFT): FP64 <= 2e-15*log2(N), FP32 <= 6e-7*log2(N).  Against the
+CPU restatement of the reference's algorithm the bound is that tolerance
+plus the restatement's own measured error (the reference's twiddle
+recurrences lose accuracy with N, to ~1e-11 in FP64 at 3*2^18).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gfft_gb300 import inputs
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def tol(n, dbl):
+    return (2e-15 if dbl else 6e-7) * max(1.0, np.log2(max(n, 2)))
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    d = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (d if d > 0 else 1.0)
+
+
+def run_gpu(torch, n, vt, tr, pl, x, batch=1, opts=None):
+    from gfft_gb300 import gfft as G
+    obj = G.TransformObject(n, G.VALUE_TYPES[vt], G.TRANSFORM_TYPES[tr], 1, G.Serial, G.PLACES[pl], batch, opts)
+    src = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    if pl == 0:
+        obj.fft(src)
+        out = src
+    else:
+        out = torch.empty_like(src)
+        obj.fft(src, out)
+    torch.cuda.synchronize()
+    r = out.cpu().numpy()
+    obj.close()
+    return r
+
+
+def packed_rfft(x):
+    """FP64 real DFT of 2n reals in the reference's packed layout."""
+    x = np.asarray(x, dtype=np.float64)
+    n = x.size // 2
+    f = np.fft.rfft(x)
+    out = np.empty(2 * n)
+    out[0], out[1] = f[0].real, f[n].real
+    out[2::2], out[3::2] = f[1:n].real, f[1:n].imag
+    return out
+
+
+def exact(oracle, x, n, tr, batch=1):
+    x = np.asarray(x, dtype=np.float64)
+    if tr in (0, 1):
+        s = 1 if tr == 0 else -1
+        if n <= 512 and batch == 1:
+            return oracle.dft_q(x, s)
+        return oracle.fft_ld(x, n, batch, s)
+    raise ValueError
+
+
+SMALL = list(range(1, 65)) + [81, 96, 100, 121, 125, 128, 243, 256, 343, 360, 500, 512, 625, 729, 1000, 1024,
+                                1536, 2048, 2187, 2401, 3000, 3072, 3125, 4096]
+PRIMES = [11, 13, 17, 19, 23, 29, 31, 37, 41, 97, 127, 257, 1009]
+MULTI = [8192, 12288, 15625, 16384, 65536, 3 * 2 ** 14, 2 ** 20, 5 ** 8]
+
+
+@pytest.mark.parametrize("dbl", [1, 0])
+@pytest.mark.parametrize("n", SMALL + PRIMES)
+def test_c2c_vs_exact(cuda, oracle, n, dbl):
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    x = inputs.uniform(1000 + n, 2 * n).astype(dt)
+    for tr in (0, 1):
+        y = run_gpu(cuda, n, vt, tr, 1, x)
+        ex = exact(oracle, x, n, tr)
+        assert rel(y, ex) <= tol(n, dbl), (n, tr, rel(y, ex))
+
+
+@pytest.mark.parametrize("dbl", [1, 0])
+@pytest.mark.parametrize("n", MULTI)
+def test_multipass_vs_exact(cuda, oracle, n, dbl):
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    x = inputs.gaussian(2000 + n, 2 * n).astype(dt)
+    for tr in (0, 1):
+        for pl in (1, 0):
+            y = run_gpu(cuda, n, vt, tr, pl, x)
+            ex = exact(oracle, x, n, tr)
+            assert rel(y, ex) <= tol(n, dbl), (n, tr, pl, rel(y, ex))
+
+
+@pytest.mark.parametrize("dbl", [1, 0])
+@pytest.mark.parametrize("n", [16, 60, 243, 1024, 3000, 4096, 8192, 786432])
+def test_vs_restatement(cuda, oracle, n, dbl):
+    """Against the reference's own algorithm restated on the CPU."""
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    x = inputs.uniform(0x5EED0000 + n, 2 * n).astype(dt)
+    ex = exact(oracle, x, n, 0)
+    ref = oracle.gfft(n, vt, 0, 1, x)
+    ref_err = rel(ref, ex)
+    y = run_gpu(cuda, n, vt, 0, 1, x)
+    assert rel(y, ref) <= tol(n, dbl) + 2 * ref_err, (n, rel(y, ref), ref_err)
+    assert rel(y, ex) <= tol(n, dbl)
+
+
+def test_golden_reference_arrays(cuda, oracle):
+    """The compiled reference's stored outputs (DOUBLE/FLOAT objects)."""
+    arr = np.load(os.path.join(GOLD, "reference_arrays.npz"))
+    checked = 0
+    for key in arr.files:
+        vt_name, tr, pl, n = key.rsplit("_", 3)
+        tr, pl, n = int(tr), int(pl), int(n)
+        dbl = "DOUBLE" in vt_name
+        dt = np.float64 if dbl else np.float32
+        x = inputs.uniform(0x5EED0000 + n, 2 * n).astype(dt)
+        vt = {"DOUBLE": 0, "FLOAT": 1, "COMPLEX_DOUBLE": 2, "COMPLEX_FLOAT": 3}[vt_name]
+        y = run_gpu(cuda, n, vt, tr, pl, x)
+        ref = arr[key]
+        if vt >= 2 and tr < 2 and pl == 1 and n % 10 == 0:
+            continue  # the reference's std::complex path is defective here (test_oracle.py)
+        assert rel(y, ref) <= tol(n, dbl) * 4, (key, rel(y, ref))
+        checked += 1
+    assert checked >= 8
+
+
+def test_golden_digests_match_within_tolerance(cuda, oracle):
+    """For the fixture sizes the GPU result is within tolerance of the
+    reference output (recomputed by the pinned restatement)."""
+    with open(os.path.join(GOLD, "reference_outputs.json")) as f:
+        entries = [e for e in json.load(f)["entries"] if e["vtype"] in ("DOUBLE", "FLOAT") and e["n"] <= 4096]
+    for e in entries[::7]:
+        dbl = e["vtype"] == "DOUBLE"
+        dt = np.float64 if dbl else np.float32
+        x = inputs.uniform(e["seed"], 2 * e["n"]).astype(dt)
+        roots = ([float.fromhex(v) for v in e["roots_re"]], [float.fromhex(v) for v in e["roots_im"]])
+        ref = oracle.gfft(e["n"], 0 if dbl else 1, e["trans"], e["place"], x, roots=roots)
+        assert oracle.digest(ref) == e["sha256"]
+        y = run_gpu(cuda, e["n"], 0 if dbl else 1, e["trans"], e["place"], x)
+        t = tol(e["n"], dbl) * 8
+        assert rel(y, ref) <= t, (e["n"], e["trans"], e["place"], rel(y, ref))
+
+
+@pytest.mark.parametrize("dbl", [1, 0])
+@pytest.mark.parametrize("n", [1, 2, 4, 8, 16, 64, 256, 1024, 4096, 8192, 1 << 15, 1 << 19])
+def test_real_forward_inverse(cuda, oracle, n, dbl):
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    x = inputs.uniform(3000 + n, 2 * n).astype(dt)
+    y = run_gpu(cuda, n, vt, 2, 0, x)
+    ex = oracle.rdft_q(x.astype(np.float64)) if n <= 256 else packed_rfft(x)
+    assert rel(y, ex) <= tol(2 * n, dbl), (n, rel(y, ex))
+    back = run_gpu(cuda, n, vt, 3, 0, y)
+    assert rel(back, x) <= 2 * tol(2 * n, dbl), (n, rel(back, x))
+    # against the restatement of the reference's IRDFT on the same spectrum
+    ri = oracle.gfft(n, vt, 3, 0, y)
+    assert rel(back, ri) <= 2 * tol(2 * n, dbl) + 2 * rel(ri, x)
+
+
+@pytest.mark.parametrize("n", [6, 12, 48, 100, 1000, 3 * 1024, 12288])
+def test_real_beyond_reference(cuda, oracle, n):
+    """Non-power-of-two and out-of-place real transforms (the reference
+    rejects both: src/gfftswap.h:282-286)."""
+    x = inputs.uniform(4000 + n, 2 * n)
+    ex = packed_rfft(x)
+    for pl in (0, 1):
+        y = run_gpu(cuda, n, 0, 2, pl, x)
+        assert rel(y, ex) <= 4 * tol(2 * n, 1), (n, pl, rel(y, ex))
+        back = run_gpu(cuda, n, 0, 3, pl, y)
+        assert rel(back, x) <= 4 * tol(2 * n, 1)
+
+
+def test_batch_equals_single(cuda, oracle):
+    for n, dbl in ((1024, 1), (4096, 0), (60, 0), (12288, 1)):
+        dt = np.float64 if dbl else np.float32
+        vt = 0 if dbl else 1
+        B = 5
+        x = inputs.uniform(77 + n, 2 * n * B).astype(dt)
+        yb = run_gpu(cuda, n, vt, 0, 1, x, batch=B)
+        for b in range(B):
+            ys = run_gpu(cuda, n, vt, 0, 1, x[2 * n * b:2 * n * (b + 1)])
+            assert np.array_equal(ys, yb[2 * n * b:2 * n * (b + 1)]), (n, b)
+
+
+def test_inplace_equals_outofplace(cuda):
+    for n in (1024, 3000, 65536, 1 << 20):
+        x = inputs.uniform(5 + n, 2 * n)
+        a = run_gpu(cuda, n, 0, 0, 0, x)
+        b = run_gpu(cuda, n, 0, 0, 1, x)
+        assert np.array_equal(a, b)
+
+
+def test_complex_dtypes_same_bytes(cuda):
+    import torch
+    from gfft_gb300 import gfft as G
+    n = 1000
+    x = inputs.uniform(9, 2 * n)
+    a = run_gpu(cuda, n, 0, 0, 1, x)
+    obj = G.TransformObject(n, G.COMPLEX_DOUBLE, G.DFT)
+    src = torch.from_numpy(x).cuda().view(torch.complex128)
+    dst = torch.empty_like(src)
+    obj.fft(src, dst)
+    b = dst.view(torch.float64).cpu().numpy()
+    assert np.array_equal(a, b)
+
+
+def test_plan_options_agree(cuda, oracle):
+    """Every autotuner knob gives the same transform within tolerance."""
+    n = 4096
+    x = inputs.uniform(31, 2 * n * 3).astype(np.float32)
+    ex = oracle.fft_ld(x, n, 3, 1)
+    for opts in ({"max_radix": 8}, {"max_radix": 4}, {"max_radix": 2}, {"radix_order": 1},
+                 {"threads_per_block": 128}, {"units_per_block": 2}, {"max_pass_len": 64}):
+        y = run_gpu(cuda, n, 1, 0, 1, x, batch=3, opts=opts)
+        assert rel(y, ex) <= tol(n, 0), (opts, rel(y, ex))
+
+
+def test_host_entry_point(cuda, oracle):
+    from gfft_gb300 import gfft as G
+    n = 2048
+    x = inputs.uniform(41, 2 * n)
+    obj = G.TransformObject(n, G.DOUBLE, G.DFT)
+    y = np.zeros_like(x)
+    obj.fft(x, y)
+    assert rel(y, oracle.fft_ld(x, n, 1, 1)) <= tol(n, 1)
+    inp = G.TransformObject(n, G.DOUBLE, G.DFT, place=G.IN_PLACE)
+    z = x.copy()
+    inp.fft(z)
+    assert np.array_equal(z, y)
+
+
+def test_error_codes(cuda):
+    import ctypes
+    from gfft_gb300 import _lib
+    from gfft_gb300 import gfft as G
+    L = _lib.lib()
+    obj = G.TransformObject(64, G.DOUBLE, G.DFT, place=G.IN_PLACE)
+    t = cuda.zeros(256, dtype=cuda.float64, device="cuda")
+    p = t.data_ptr()
+    assert L.gfft_exec(obj._h, None, ctypes.c_void_p(p), None) == 7
+    assert L.gfft_exec(obj._h, ctypes.c_void_p(p + 8), ctypes.c_void_p(p + 8), None) == 8
+    assert L.gfft_exec(obj._h, ctypes.c_void_p(p), ctypes.c_void_p(p + 1024), None) == 4
+    assert L.gfft_exec(None, ctypes.c_void_p(p), ctypes.c_void_p(p), None) == 11
+    assert L.gfft_exec(obj._h, ctypes.c_void_p(p), ctypes.c_void_p(p), None) == 0
+    h = ctypes.c_void_p()
+    assert L.gfft_create(ctypes.byref(h), 2 * 4099, 1, 0, 1, 0, 1, 1) == 1
+    assert L.gfft_create(ctypes.byref(h), 64, 0, 0, 2, 0, 1, 1) == 5
+    cuda.cuda.synchronize()
+    # the context is still usable
+    y = run_gpu(cuda, 16, 0, 0, 1, inputs.uniform(1, 32))
+    assert np.isfinite(y).all()
+
+
+# ---- full-size configurations, size-independent properties --------------
+def test_c1_fp64_1024_batch4096_inplace_roundtrip(cuda, oracle):
+    import torch
+    from gfft_gb300 import gfft as G
+    n, B = 1024, 4096
+    x = inputs.uniform(0x5EED0001, 2 * n * B)
+    t = torch.from_numpy(x).cuda()
+    f = G.TransformObject(n, G.DOUBLE, G.DFT, place=G.IN_PLACE, batch=B)
+    f.fft(t)
+    torch.cuda.synchronize()
+    y = t.cpu().numpy()
+    for b in (0, 1, 2047, 4095):  # spot transforms against the exact oracle
+        seg = slice(2 * n * b, 2 * n * (b + 1))
+        assert rel(y[seg], oracle.fft_ld(x[seg], n, 1, 1)) <= tol(n, 1)
+    f.ifft(t)
+    torch.cuda.synchronize()
+    assert rel(t.cpu().numpy(), x) <= 2 * tol(n, 1)
+
+
+@pytest.mark.parametrize("n", [3 * 2 ** 18, 5 ** 8, 2 ** 10 * 3 ** 5])
+@pytest.mark.parametrize("dbl", [1, 0])
+def test_c2_mixed_radix_batch8(cuda, oracle, n, dbl):
+    dt = np.float64 if dbl else np.float32
+    B = 8
+    x = inputs.gaussian(0x5EED0002 + n, 2 * n * B).astype(dt)
+    y = run_gpu(cuda, n, 0 if dbl else 1, 0, 1, x, batch=B)
+    seg = slice(2 * n * 5, 2 * n * 6)
+    assert rel(y[seg], oracle.fft_ld(x[seg], n, 1, 1)) <= tol(n, dbl)
+    # Parseval over the batch
+    e_in = np.sum(x.astype(np.float64) ** 2) * n
+    e_out = np.sum(y.astype(np.float64) ** 2)
+    assert abs(e_out / e_in - 1) <= 10 * tol(n, dbl)
+    back = run_gpu(cuda, n, 0 if dbl else 1, 1, 1, y, batch=B)
+    assert rel(back, x) <= 2 * tol(n, dbl)
+
+
+def test_c2b_real_2pow20_batch16(cuda, oracle):
+    n, B = 1 << 19, 16
+    x = inputs.uniform(0x5EED0003, 2 * n * B)
+    y = run_gpu(cuda, n, 0, 2, 0, x, batch=B)
+    seg = slice(2 * n * 3, 2 * n * 4)
+    ref = oracle.gfft(n, 0, 2, 0, x[seg])
+    exact_packed = packed_rfft(x[seg])
+    assert rel(y[seg], exact_packed) <= tol(2 * n, 1) * 2
+    assert rel(y[seg], ref) <= tol(2 * n, 1) * 2 + 2 * rel(ref, exact_packed)
+    back = run_gpu(cuda, n, 0, 3, 0, y, batch=B)
+    assert rel(back, x) <= 2 * tol(2 * n, 1)
+
+
+def test_c3_fp32_4096_batch65536(cuda, oracle):
+    import torch
+    from gfft_gb300 import gfft as G
+    n, B = 4096, 65536
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    x = torch.randn(2 * n * B, device="cuda", dtype=torch.float32, generator=g)
+    y = torch.empty_like(x)
+    G.TransformObject(n, G.FLOAT, G.DFT, batch=B).fft(x, y)
+    torch.cuda.synchronize()
+    for b in (0, 12345, 65535):
+        seg = slice(2 * n * b, 2 * n * (b + 1))
+        xs = x[seg].cpu().numpy().astype(np.float64)
+        assert rel(y[seg].cpu().numpy(), oracle.fft_ld(xs, n, 1, 1)) <= tol(n, 0)
+    z = torch.empty_like(x)
+    G.TransformObject(n, G.FLOAT, G.IDFT, batch=B).fft(y, z)
+    torch.cuda.synchronize()
+    assert (torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x)).item() <= 2 * tol(n, 0)
+
+
+def test_c3_fp32_2pow24(cuda, oracle):
+    import torch
+    from gfft_gb300 import gfft as G
+    n = 1 << 24
+    x = inputs.gaussian(0x5EED0004, 2 * n).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xt)
+    G.TransformObject(n, G.FLOAT, G.DFT).fft(xt, y)
+    torch.cuda.synchronize()
+    yn = y.cpu().numpy()
+    bins = np.array([0, 1, 2, 777, n // 2, n - 1, 123456, 9999999])
+    exb = oracle.dft_bins_q(x.astype(np.float64), bins, 1)
+    got = np.empty(2 * len(bins))
+    got[0::2], got[1::2] = yn[2 * bins], yn[2 * bins + 1]
+    scale = np.sqrt(np.sum(x.astype(np.float64) ** 2))  # ~|X_k| for noise input
+    assert np.max(np.abs(got - exb)) / scale <= 10 * tol(n, 0)
+    e_in = np.sum(x.astype(np.float64) ** 2) * n
+    assert abs(np.sum(yn.astype(np.float64) ** 2) / e_in - 1) <= 10 * tol(n, 0)

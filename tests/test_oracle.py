@@ -1,0 +1,131 @@
+"""CPU: the oracle against the compiled reference's golden fixtures.
+
+The restatement (oracle/gfft_restate.cpp), given the reference's own
+per-level root constants, must reproduce the reference's output bytes
+exactly (SHA-256 equal) for every fixture entry; the exact references
+(binary128 DFT, long-double FFT) must agree with each other, and with the
+reference within its own error.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gfft_gb300 import inputs
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _entries():
+    with open(os.path.join(GOLD, "reference_outputs.json")) as f:
+        return json.load(f)["entries"]
+
+
+ENTRIES = _entries()
+REAL_ENTRIES = [e for e in ENTRIES if e["vtype"] in ("DOUBLE", "FLOAT")]
+
+
+def _input(e):
+    dt = np.float64 if e["vtype"] in ("DOUBLE", "COMPLEX_DOUBLE") else np.float32
+    return inputs.uniform(e["seed"], 2 * e["n"]).astype(dt)
+
+
+def test_fixture_inventory():
+    kinds = {(e["vtype"], e["trans"], e["place"]) for e in ENTRIES}
+    # every value type x {DFT, IDFT} x {in, out of place} and real in place
+    for vt in ("DOUBLE", "FLOAT", "COMPLEX_DOUBLE", "COMPLEX_FLOAT"):
+        for tr in (0, 1):
+            for pl in (0, 1):
+                assert (vt, tr, pl) in kinds
+        assert (vt, 2, 0) in kinds and (vt, 3, 0) in kinds
+    assert {786432, 390625, 248832, 524288} <= {e["n"] for e in ENTRIES}
+
+
+@pytest.mark.parametrize("e", REAL_ENTRIES, ids=lambda e: "%s-t%d-p%d-n%d" % (e["vtype"], e["trans"], e["place"],
+                                                                              e["n"]))
+def test_restatement_bit_exact(oracle, e):
+    x = _input(e)
+    vt = 0 if e["vtype"] == "DOUBLE" else 1
+    roots = ([float.fromhex(v) for v in e["roots_re"]], [float.fromhex(v) for v in e["roots_im"]])
+    y = oracle.gfft(e["n"], vt, e["trans"], e["place"], x, roots=roots)
+    assert oracle.digest(y) == e["sha256"]
+
+
+def _std_complex_defect(n, place):
+    """The reference's std::complex path (src/gfftstdspec.h, src/gfftstdalg.h)
+    is wrong out of place when N has both the factors 2 and 5 (N = 10, 20,
+    30, 60, 100, 120, 1000: relative error 0.1-0.6 against the exact DFT)."""
+    return place == 1 and n % 2 == 0 and n % 5 == 0
+
+
+def test_complex_value_types_match_restatement(oracle):
+    """COMPLEX_* objects have the same bytes as DOUBLE/FLOAT; where the
+    reference's std::complex path is correct its stored arrays agree with the
+    restatement to a few ulps, and where it is defective (see above) they
+    are far from the exact DFT, which the library does not reproduce."""
+    arr = np.load(os.path.join(GOLD, "reference_arrays.npz"))
+    seen_defect = 0
+    for key in arr.files:
+        vt, tr, pl, n = key.rsplit("_", 3)
+        tr, pl, n = int(tr), int(pl), int(n)
+        ref = arr[key]
+        dt = np.float64 if "DOUBLE" in vt else np.float32
+        x = inputs.uniform(0x5EED0000 + n, 2 * n).astype(dt)
+        y = oracle.gfft(n, 0 if dt == np.float64 else 1, tr, pl, x)
+        eps = np.finfo(dt).eps
+        err = np.linalg.norm(y.astype(np.float64) - ref) / np.linalg.norm(ref.astype(np.float64))
+        if vt.startswith("COMPLEX") and tr < 2 and _std_complex_defect(n, pl):
+            exact = oracle.dft_q(x.astype(np.float64), 1 if tr == 0 else -1)
+            assert np.linalg.norm(ref - exact) / np.linalg.norm(exact) > 1e-2
+            seen_defect += 1
+            continue
+        assert err < 64 * eps * max(1, np.log2(n)), (key, err)
+    assert seen_defect >= 1
+
+
+def test_std_complex_defect_family(oracle):
+    """Pin the defect's extent with the compiled reference when present."""
+    ref = oracle.ref_lib()
+    if ref is None:
+        pytest.skip("compiled reference not available")
+    for n in (10, 20, 60, 100, 12, 15, 16, 25, 125, 243):
+        x = inputs.uniform(7 + n, 2 * n)
+        y = np.zeros_like(x)
+        assert ref.ref_exec_COMPLEX_DOUBLE(n, 0, 1, x.ctypes.data, y.ctypes.data) == 0
+        exact = oracle.dft_q(x, 1)
+        bad = np.linalg.norm(y - exact) / np.linalg.norm(exact) > 1e-4
+        assert bad == _std_complex_defect(n, 1), n
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 12, 17, 64, 100, 243, 1000])
+def test_exact_references_agree(oracle, n):
+    x = inputs.uniform(11 + n, 2 * n)
+    a = oracle.dft_q(x, 1)
+    b = oracle.fft_ld(x, n, 1, 1)
+    assert np.max(np.abs(a - b)) <= 1e-15 * max(1.0, np.max(np.abs(a)))
+    ai = oracle.dft_q(x, -1)
+    bi = oracle.fft_ld(x, n, 1, -1)
+    assert np.max(np.abs(ai - bi)) <= 1e-16 * max(1.0, np.max(np.abs(ai))) * n
+
+
+@pytest.mark.parametrize("n", [2, 8, 64, 256])
+def test_real_transform_definition(oracle, n):
+    """RDFT of 2n reals = packed half spectrum of the direct real DFT."""
+    x = inputs.uniform(23 + n, 2 * n)
+    exact = oracle.rdft_q(x)
+    y = oracle.gfft(n, 0, 2, 0, x)
+    assert np.max(np.abs(y - exact)) <= 1e-13 * max(1.0, np.max(np.abs(exact)))
+    back = oracle.gfft(n, 0, 3, 0, y)
+    assert np.max(np.abs(back - x)) <= 1e-14
+
+
+def test_reference_accuracy_large_n(oracle):
+    """The reference's own FP64 error at 3*2^18 (its radix-2 twiddle
+    recurrence runs in double, src/gfftalg.h:249-265)."""
+    n = 786432
+    x = inputs.uniform(0x5EED0000 + n, 2 * n)
+    y = oracle.gfft(n, 0, 0, 1, x)
+    exact = oracle.fft_ld(x, n, 1, 1)
+    rel = np.linalg.norm(y - exact) / np.linalg.norm(exact)
+    assert rel < 1e-10
