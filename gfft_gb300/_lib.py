@@ -22,13 +22,15 @@ STATUS_NAMES = {
 
 # every symbol the header declares, checked by the CPU tests
 EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
-            "gfft_get_info", "gfft_plan_query", "gfft_version"]
+            "gfft_get_info", "gfft_plan_query", "gfft_get_device_status", "gfft_selftest_bounded_wait",
+            "gfft_version"]
 
 
 class PlanOpts(ctypes.Structure):
     _fields_ = [("radix_order", ctypes.c_int), ("max_radix", ctypes.c_int), ("threads_per_block", ctypes.c_int),
                 ("units_per_block", ctypes.c_int), ("max_pass_len", ctypes.c_int),
-                ("kernel_variant", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("kernel_variant", ctypes.c_int), ("stages", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -76,6 +78,8 @@ def lib():
         L.gfft_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
         L.gfft_plan_query.argtypes = [u64, ci, ci, ci, u64, ctypes.POINTER(PlanOpts), ctypes.POINTER(PlanInfo)]
         L.gfft_version.restype = ctypes.c_char_p
+        L.gfft_get_device_status.argtypes = [vp, ctypes.POINTER(ci)]
+        L.gfft_selftest_bounded_wait.argtypes = [ctypes.c_longlong, ctypes.POINTER(ci)]
         for name in EXPORTED:
             getattr(L, name).restype = getattr(L, name).restype or ci
         L.gfft_strerror.restype = ctypes.c_char_p

@@ -20,6 +20,10 @@
 extern "C" int gfft_engine_setup(int dbl, size_t max_smem);
 extern "C" int gfft_engine_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                   cudaStream_t stream);
+extern "C" int gfft_fast_setup(int dbl, size_t max_smem);
+extern "C" int gfft_fast_occupancy(int dbl, int threads, size_t smem);
+extern "C" int gfft_fast_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                cudaStream_t stream);
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
 
@@ -34,6 +38,8 @@ struct gfft_plan {
   // staging buffers for gfft_exec_host, allocated on first use
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
+  int* d_status = nullptr;     // device status word of this handle's kernels
+  unsigned grid[GFFT_MAXG] = {0, 0, 0, 0};  // persistent grid of fast-path passes
   unsigned magic = 0x6FF7B300u;
 };
 
@@ -53,6 +59,7 @@ int setup_device_once(int dbl) {
   int maxopt = 0;
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (gfft_engine_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
+  if (gfft_fast_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (dev < 64) done[dbl][dev] = true;
   return GFFT_OK;
 }
@@ -75,6 +82,9 @@ int parse_opts(const gfft_plan_opts* opts, PlanOpts& po) {
   po.units = opts->units_per_block;
   po.max_pass_len = opts->max_pass_len;
   po.variant = opts->kernel_variant;
+  if (opts->stages < 0 || opts->stages > 8 || opts->blocks_per_sm < 0 || opts->blocks_per_sm > 32)
+    return GFFT_E_INVALID_PLAN;
+  po.stages = opts->stages;
   return GFFT_OK;
 }
 
@@ -190,6 +200,24 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
     delete h;
     return GFFT_E_CUDA;
   }
+  if (cudaMalloc((void**)&h->d_status, 256) != cudaSuccess || cudaMemset(h->d_status, 0, 256) != cudaSuccess) {
+    cudaFree(h->d_tab);
+    delete h;
+    return GFFT_E_ALLOC;
+  }
+  {
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
+    for (int g = 0; g < h->hp.nglobal; ++g) {
+      const GlobalPass& gp = h->hp.gp[g];
+      if (gp.variant != 2) continue;
+      int per = (opts && opts->blocks_per_sm) ? opts->blocks_per_sm : gfft_fast_occupancy(dbl, gp.threads, gp.smem);
+      if (per < 1) per = 1;
+      long long grid = (long long)nsm * per;
+      if (grid > gp.ntiles) grid = gp.ntiles;
+      h->grid[g] = (unsigned)std::max<long long>(grid, 1);
+    }
+  }
   if (h->hp.n_ws > 0) {
     h->ws_bytes = h->hp.ws_elems * elem_bytes(dbl);
     for (int i = 0; i < h->hp.n_ws; ++i)
@@ -216,6 +244,7 @@ int gfft_destroy(gfft_handle h) {
   for (int i = 0; i < 2; ++i)
     if (h->d_ws[i]) cudaFree(h->d_ws[i]);
   if (h->d_stage) cudaFree(h->d_stage);
+  if (h->d_status) cudaFree(h->d_status);
   delete h;
   return GFFT_OK;
 }
@@ -334,6 +363,16 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     // conjugates inside its own load.
     a.conj = inverse ? 1 : 0;
     a.scale = (inverse && last) ? 1.0 / (double)n : 1.0;
+    a.status = h->d_status;
+    if (gp.variant == 2) {
+      a.ntiles = gp.ntiles;
+      a.stages = gp.stages;
+      a.tile_bytes = gp.tile_bytes;
+      a.spin_limit = 1LL << 26;
+      a.debug_no_issue = 0;
+      if (gfft_fast_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      continue;
+    }
     long long grid = (a.nunits + a.W - 1) / a.W;
     if (grid > 0x7FFFFFFFLL) return GFFT_E_INVALID_SIZE;
     if (gfft_engine_launch(dbl, &a, (unsigned)grid, (unsigned)gp.threads, gp.smem, stream) != 0)
@@ -343,6 +382,62 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     if (gfft_real_pass_launch(dbl, dst, n, batch, 1, tab + p.rtw_off * esz, stream) != 0) return GFFT_E_CUDA;
   }
   return GFFT_OK;
+}
+
+int gfft_get_device_status(gfft_handle h, int* status) {
+  if (!valid(h)) return GFFT_E_INVALID_HANDLE;
+  if (!status) return GFFT_E_NULL_POINTER;
+  if (cudaDeviceSynchronize() != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaMemcpy(status, h->d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaMemset(h->d_status, 0, sizeof(int)) != cudaSuccess) return GFFT_E_CUDA;
+  return GFFT_OK;
+}
+
+int gfft_selftest_bounded_wait(long long spin_limit, int* status) {
+  if (!status) return GFFT_E_NULL_POINTER;
+  if (spin_limit < 1) return GFFT_E_INVALID_PLAN;
+  gfft_handle h = nullptr;
+  int st = gfft_create(&h, 4096, 1, 0, 1, 0, 1, 64);
+  if (st != GFFT_OK) return st;
+  const GlobalPass& gp = h->hp.gp[0];
+  if (gp.variant != 2) {
+    gfft_destroy(h);
+    return GFFT_E_INVALID_PLAN;
+  }
+  void* buf = nullptr;
+  const size_t bytes = (size_t)4096 * 64 * 8;
+  if (cudaMalloc(&buf, 2 * bytes) != cudaSuccess) {
+    gfft_destroy(h);
+    return GFFT_E_ALLOC;
+  }
+  EngineArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.in = buf;
+  a.out = (char*)buf + bytes;
+  a.N = 4096;
+  a.L = 4096;
+  a.stride = 1;
+  a.nunits = 64;
+  a.gNs = 1;
+  a.tw = h->d_tab;
+  a.pad_shift = 4;
+  a.Lp = 4096 + 256 + 1;
+  a.W = gp.units;
+  a.mode = 0;
+  a.npass = gp.npass;
+  for (int i = 0; i < gp.npass; ++i) a.pass[i] = gp.pass[i];
+  a.scale = 1.0;
+  a.status = h->d_status;
+  a.ntiles = gp.ntiles;
+  a.stages = gp.stages;
+  a.tile_bytes = gp.tile_bytes;
+  a.spin_limit = spin_limit;
+  a.debug_no_issue = 1;  // nothing ever arrives on the barriers
+  st = gfft_fast_launch(h->hp.dbl, &a, 4, (unsigned)gp.threads, gp.smem, 0) != 0 ? GFFT_E_CUDA : GFFT_OK;
+  if (st == GFFT_OK) st = gfft_get_device_status(h, status);
+  cudaFree(buf);
+  gfft_destroy(h);
+  return st;
 }
 
 int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {

@@ -49,6 +49,13 @@ struct EngineArgs {
   int real;           // 0 none, 1 real forward post pass, 2 real inverse pre pass
   int pad_shift;      // shared-memory padding: one slot per 2^pad_shift elements
   double scale;       // output scale
+  // register-resident pipelined path (variant 2)
+  int* status;        // device status word (0 ok, GFFT_E_TIMEOUT on a wait that ran out)
+  long long ntiles;   // tiles of W contiguous transforms
+  int stages;         // TMA stages per block
+  int tile_bytes;     // bytes of one tile (multiple of 16)
+  long long spin_limit;  // bound on every mbarrier wait (try_wait iterations)
+  int debug_no_issue; // test hook: never issue the copies, so the first wait runs out
   BlockPass pass[GFFT_MAXP];
 };
 
@@ -62,6 +69,9 @@ struct GlobalPass {
   int npass;
   BlockPass pass[GFFT_MAXP];
   size_t smem;
+  int stages;     // variant 2: TMA pipeline depth
+  long long ntiles;
+  int tile_bytes;
 };
 
 struct PlanOpts {
@@ -71,6 +81,7 @@ struct PlanOpts {
   int units = 0;
   int max_pass_len = 0;
   int variant = 0;
+  int stages = 0;
 };
 
 struct HostPlan {

@@ -221,6 +221,31 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     gp.threads = thr;
     gp.variant = 1;
     gp.smem = (size_t)(2LL * gp.units * padded(gp.L) * esz);
+    // register-resident TMA-pipelined path: power-of-two single pass whose
+    // radices divide 16, 16 values per thread
+    bool pow2ok = gp.mode == 0 && trans < 2 && gp.L >= 16 && (gp.L & (gp.L - 1)) == 0 && o.variant != 1;
+    for (int i = 0; i < gp.npass && pow2ok; ++i) pow2ok = (16 % gp.pass[i].R) == 0;
+    if (pow2ok) {
+      long long target = 4096 * 8 / esz;  // ~32 KB tiles
+      int W = o.units > 0 ? o.units : (int)std::max<long long>(1, target / gp.L);
+      W = (int)std::min<long long>(W, batch);
+      while (W > 1 && (long long)W * gp.L / 16 > 512) --W;
+      // threads = W*L/16 must be a whole number of warps
+      while (W > 1 && ((long long)W * gp.L / 16) % 32 != 0) --W;
+      const long long T = (long long)W * gp.L / 16;
+      const long long tile = (long long)W * gp.L * esz;
+      if (T >= 32 && T % 32 == 0 && T <= 512 && tile % 16 == 0) {
+        int S = o.stages > 0 ? o.stages : 2;
+        gp.variant = 2;
+        gp.units = W;
+        gp.threads = (int)T;
+        gp.stages = S;
+        gp.tile_bytes = (int)tile;
+        gp.ntiles = (batch + W - 1) / W;
+        const long long tb_al = (tile + 127) & ~127LL;
+        gp.smem = (size_t)(S * tb_al + ((W * padded(gp.L) * esz + 7) & ~7LL) + 8 * S);
+      }
+    }
     Ns *= gp.L;
   }
   plan.tw_count = tw;

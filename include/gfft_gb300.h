@@ -79,7 +79,9 @@ typedef struct gfft_plan_opts {
   int units_per_block;    /* transforms (single-pass) or lanes (multi-pass) per block */
   int max_pass_len;       /* cap on one pass's in-block length (forces more passes) */
   int kernel_variant;     /* 0 = auto, 1 = generic engine, 2 = register-resident fast path */
-  int reserved[6];
+  int stages;             /* bulk-copy pipeline depth of the fast path (0 = 2) */
+  int blocks_per_sm;      /* persistent blocks per SM of the fast path (0 = occupancy) */
+  int reserved[4];
 } gfft_plan_opts;
 
 int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim,
@@ -124,6 +126,17 @@ int gfft_get_info(gfft_handle handle, gfft_plan_info* info);
  * (the reference plans at compile time). */
 int gfft_plan_query(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
                     const gfft_plan_opts* opts, gfft_plan_info* info);
+
+/* Status word the device code of this handle's kernels writes (a bounded
+ * wait that ran out sets GFFT_E_TIMEOUT).  Synchronises the handle's device,
+ * returns the word in *status and clears it. */
+int gfft_get_device_status(gfft_handle handle, int* status);
+
+/* Self-test of the bounded waits: launches the pipelined kernel with its
+ * copies switched off, so that its first wait (limited to `spin_limit`
+ * try-wait rounds) runs out; returns the status word it wrote (expected
+ * GFFT_E_TIMEOUT) in *status.  No reference counterpart. */
+int gfft_selftest_bounded_wait(long long spin_limit, int* status);
 
 /* Library version string. */
 const char* gfft_version(void);
