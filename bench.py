@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--batch", type=int, default=BATCH)
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     return p.parse_args()
 
 
@@ -251,7 +252,7 @@ def main():
 
     # end to end through the C ABI host entry point, pinned host buffers
     e2e = None
-    if rank == 0 or world > 1:
+    if not args.no_e2e:
         hx = x.cpu().pin_memory()
         hy = torch.empty_like(hx).pin_memory()
         obj.fft(hx, hy)  # allocates the staging buffer once
