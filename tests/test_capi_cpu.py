@@ -125,3 +125,14 @@ def test_factory_unknown_combination_raises():
 
 def test_plan_opts_layout():
     assert ctypes.sizeof(_lib.PlanOpts) == 12 * 4
+
+
+def test_cpp_facade_factory_errors():
+    """include/gfft.h compiles as the reference's user code does and throws
+    TransformFactoryError for unknown combinations (no GPU needed)."""
+    import subprocess
+    from tests.cpp import build_facade
+    exe = build_facade.build()
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "facade ok (cpu)" in r.stdout

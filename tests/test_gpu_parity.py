@@ -398,3 +398,12 @@ def test_device_status_clean_after_runs(cuda):
     st = ctypes.c_int(-1)
     assert _lib.lib().gfft_get_device_status(obj._h, ctypes.byref(st)) == 0
     assert st.value == 0
+
+
+def test_cpp_facade_on_gpu(cuda):
+    import subprocess
+    from tests.cpp import build_facade
+    exe = build_facade.build()
+    r = subprocess.run([exe, "gpu"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "facade ok (gpu)" in r.stdout
