@@ -24,6 +24,7 @@
 
 #include "butterflies.cuh"
 #include "plan.h"
+#include "tma.cuh"
 
 namespace gfft {
 
@@ -33,35 +34,6 @@ template <typename T> struct PadShift;
 template <> struct PadShift<float> { static constexpr int v = 4; };
 template <> struct PadShift<double> { static constexpr int v = 3; };
 template <typename T> __device__ __forceinline__ int pad(int s) { return s + (s >> PadShift<T>::v); }
-
-__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t phase) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase, long long limit) {
-  for (long long i = 0; i < limit; ++i)
-    if (mbar_try(bar, phase)) return true;
-  return false;
-}
 
 // Q = 16/R butterflies per thread; butterfly q of thread t is b = t + q*T
 template <typename T, int R>

@@ -1,0 +1,299 @@
+// Length-specialised register-resident TMA-pipelined FFT (variant 3).
+//
+// The same pipeline as fft_fast.cu (persistent blocks, tiles of W whole
+// transforms streamed into shared memory by 1-D bulk async copies, 16 values
+// per thread, in-block Stockham passes in shared memory, the last pass
+// stored straight to global memory), but with the power-of-two length L a
+// template parameter: the pass radices, butterfly strides and twiddle strides
+// are compile-time constants, so every shared-memory access is a register
+// base plus an immediate offset and the index arithmetic per leg vanishes.
+// The tile holds 4096 (FP32) or 2048 (FP64) complex values, W = tile / L.
+//
+// Pass order for L = 2^a: radix 16 while four bits remain, then 8 / 4 / 2,
+// matching the planner's default (planner.cpp block_radices).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "butterflies.cuh"
+#include "plan.h"
+#include "tma.cuh"
+
+namespace gfft {
+namespace spec {
+
+constexpr int lg2(int x) { return x <= 1 ? 0 : 1 + lg2(x / 2); }
+constexpr int npass_of(int L) {
+  return (lg2(L) % 4 == 0) ? lg2(L) / 4 : (lg2(L) % 4 == 1 ? (lg2(L) / 4 >= 1 ? lg2(L) / 4 + 1 : 1) : lg2(L) / 4 + 1);
+}
+constexpr int radix_of(int L, int p) {
+  return (lg2(L) % 4 == 0)   ? 16
+         : (lg2(L) % 4 == 1) ? (lg2(L) / 4 == 0 ? 2 : (p < lg2(L) / 4 - 1 ? 16 : (p == lg2(L) / 4 - 1 ? 8 : 4)))
+         : (lg2(L) % 4 == 2) ? (p < lg2(L) / 4 ? 16 : 4)
+                             : (p < lg2(L) / 4 ? 16 : 8);
+}
+constexpr int ns_of(int L, int p) { return p == 0 ? 1 : ns_of(L, p - 1) * radix_of(L, p - 1); }
+
+template <typename T> struct Cfg;
+template <> struct Cfg<float> {
+  static constexpr int TILE = 4096;
+  static constexpr int PS = 4;
+};
+template <> struct Cfg<double> {
+  static constexpr int TILE = 2048;
+  static constexpr int PS = 3;
+};
+
+template <typename T> __device__ __forceinline__ constexpr int padi(int s) { return s + (s >> Cfg<T>::PS); }
+
+// pass P: read the legs of this thread's butterflies
+template <typename T, int L, int P, bool FROM_STAGE>
+__device__ __forceinline__ void sread(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* src) {
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NT = Cfg<T>::TILE / 16;
+  constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int b = threadIdx.x + q * NT;
+    const int lane = b / NB;
+    const int j = b % NB;
+    if (FROM_STAGE) {
+      const typename Vec<T>::t* s = src + lane * L + j;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[q * R + r] = s[r * NB];
+    } else {
+      const typename Vec<T>::t* s = src + lane * LP;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[q * R + r] = s[padi<T>(j + r * NB)];
+    }
+  }
+}
+
+template <typename T, int L, int P>
+__device__ __forceinline__ void scompute(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* __restrict__ tw,
+                                         int twoff) {
+  typedef typename Vec<T>::t V;
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NS = ns_of(L, P), NT = Cfg<T>::TILE / 16;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    if constexpr (NS > 1) {
+      const int j = (threadIdx.x + q * NT) % NB;
+      const V* t = tw + twoff + (j % NS);
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], __ldg(t + (r - 1) * NS));
+    }
+    dft<T, V, R>(&v[q * R]);
+  }
+}
+
+template <typename T, int L, int P>
+__device__ __forceinline__ void swrite(const typename Vec<T>::t (&v)[16], typename Vec<T>::t* work) {
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NS = ns_of(L, P), NT = Cfg<T>::TILE / 16;
+  constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int b = threadIdx.x + q * NT;
+    const int lane = b / NB;
+    const int j = b % NB;
+    const int k = j % NS;
+    const int base = (j - k) * R + k;
+    typename Vec<T>::t* d = work + lane * LP;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[padi<T>(base + r * NS)] = v[q * R + r];
+  }
+}
+
+template <typename T, int L, int P>
+__device__ __forceinline__ void sstore(const typename Vec<T>::t (&v)[16], typename Vec<T>::t* out, int units,
+                                       bool conj, T sc) {
+  typedef typename Vec<T>::t V;
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NT = Cfg<T>::TILE / 16;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int b = threadIdx.x + q * NT;
+    const int lane = b / NB;
+    const int j = b % NB;
+    if (lane >= units) continue;
+    V* d = out + lane * L + j;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      V x = v[q * R + r];
+      if (conj) x = cconj(x);
+      d[r * NB] = cscale(x, sc);
+    }
+  }
+}
+
+// middle passes 1 .. NP-2 (in place on `work`) and the last pass
+template <typename T, int L, int P>
+__device__ __forceinline__ void rest(typename Vec<T>::t (&v)[16], typename Vec<T>::t* work,
+                                     const typename Vec<T>::t* tw, const BlockPass* passes, typename Vec<T>::t* out,
+                                     int units, bool conj, T sc) {
+  constexpr int NP = npass_of(L);
+  if constexpr (P < NP) {
+    sread<T, L, P, false>(v, work);
+    scompute<T, L, P>(v, tw, passes[P].tw);
+    if constexpr (P == NP - 1) {
+      sstore<T, L, P>(v, out, units, conj, sc);
+    } else {
+      __syncthreads();
+      swrite<T, L, P>(v, work);
+      __syncthreads();
+      rest<T, L, P + 1>(v, work, tw, passes, out, units, conj, sc);
+    }
+  }
+}
+
+}  // namespace spec
+
+template <typename T, int L>
+__global__ void __launch_bounds__(spec::Cfg<T>::TILE / 16, 1) spec_kernel(const __grid_constant__ EngineArgs a) {
+  using namespace spec;
+  using namespace fast;
+  typedef typename Vec<T>::t V;
+  constexpr int TILE = Cfg<T>::TILE, W = TILE / L, NP = npass_of(L);
+  constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
+  constexpr int TB = TILE * (int)sizeof(V);  // bytes of a full tile (multiple of 128)
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int S = a.stages;
+  unsigned char* stage0 = smem;
+  V* work = reinterpret_cast<V*>(smem + (size_t)S * TB);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)S * TB + (((size_t)W * LP * sizeof(V) + 7) & ~7));
+  const V* in = (const V*)a.in;
+  V* out = (V*)a.out;
+  const V* tw = (const V*)a.tw;
+  const bool conj = a.conj != 0;
+  const T sc = (T)a.scale;
+  const long long G = gridDim.x;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(saddr(&bars[s]), 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  auto issue = [&](long long tile, int s) {
+    const long long u0 = tile * W;
+    const long long left = a.nunits - u0;
+    const int units = left < W ? (int)left : W;
+    const uint32_t bytes = (uint32_t)units * (uint32_t)L * (uint32_t)sizeof(V);
+    const uint32_t bar = saddr(&bars[s]);
+    mbar_expect_tx(bar, bytes);
+    bulk_load(saddr(stage0 + (size_t)s * TB), in + u0 * L, bytes, bar);
+  };
+  if (threadIdx.x == 0 && !a.debug_no_issue)
+    for (int s = 0; s < S; ++s) {
+      const long long tile = blockIdx.x + (long long)s * G;
+      if (tile < a.ntiles) issue(tile, s);
+    }
+
+  int it = 0;
+  V v[16];
+  for (long long tile = blockIdx.x; tile < a.ntiles; tile += G, ++it) {
+    const int s = it % S;
+    const uint32_t ph = (uint32_t)((it / S) & 1);
+    const bool ok = mbar_wait_bounded(saddr(&bars[s]), ph, a.spin_limit);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(a.status, 13 /* GFFT_E_TIMEOUT */);
+        if (!a.debug_no_issue)
+          for (int k = 1; k < S; ++k) {
+            const long long t2 = tile + (long long)k * G;
+            if (t2 >= a.ntiles) break;
+            const int j = it + k;
+            mbar_wait_bounded(saddr(&bars[j % S]), (uint32_t)((j / S) & 1), a.spin_limit);
+          }
+      }
+      return;
+    }
+    const long long u0 = tile * W;
+    const long long left = a.nunits - u0;
+    const int units = left < W ? (int)left : W;
+    const V* st = reinterpret_cast<const V*>(stage0 + (size_t)s * TB);
+    V* o = out + u0 * L;
+
+    sread<T, L, 0, true>(v, st);
+    if (conj)
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = cconj(v[i]);
+    scompute<T, L, 0>(v, tw, a.pass[0].tw);
+    __syncthreads();  // stage s read by every thread; the previous tile's reads of `work` are done
+    if (threadIdx.x == 0 && !a.debug_no_issue) {
+      const long long nt = tile + (long long)S * G;
+      if (nt < a.ntiles) issue(nt, s);
+    }
+    if constexpr (NP == 1) {
+      sstore<T, L, 0>(v, o, units, conj, sc);
+    } else {
+      swrite<T, L, 0>(v, work);
+      __syncthreads();
+      rest<T, L, 1>(v, work, tw, a.pass, o, units, conj, sc);
+    }
+  }
+}
+
+}  // namespace gfft
+
+namespace {
+template <typename T, int L>
+int spec_setup_one(size_t max_smem) {
+  return cudaFuncSetAttribute(gfft::spec_kernel<T, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem) ==
+                 cudaSuccess
+             ? 0
+             : 1;
+}
+template <typename T>
+int spec_setup_all(size_t m) {
+  int e = 0;
+  e |= spec_setup_one<T, 16>(m);
+  e |= spec_setup_one<T, 32>(m);
+  e |= spec_setup_one<T, 64>(m);
+  e |= spec_setup_one<T, 128>(m);
+  e |= spec_setup_one<T, 256>(m);
+  e |= spec_setup_one<T, 512>(m);
+  e |= spec_setup_one<T, 1024>(m);
+  e |= spec_setup_one<T, 2048>(m);
+  return e;
+}
+template <typename T>
+const void* spec_fn(int L) {
+  switch (L) {
+    case 16: return (const void*)gfft::spec_kernel<T, 16>;
+    case 32: return (const void*)gfft::spec_kernel<T, 32>;
+    case 64: return (const void*)gfft::spec_kernel<T, 64>;
+    case 128: return (const void*)gfft::spec_kernel<T, 128>;
+    case 256: return (const void*)gfft::spec_kernel<T, 256>;
+    case 512: return (const void*)gfft::spec_kernel<T, 512>;
+    case 1024: return (const void*)gfft::spec_kernel<T, 1024>;
+    case 2048: return (const void*)gfft::spec_kernel<T, 2048>;
+    case 4096: return sizeof(T) == 4 ? (const void*)gfft::spec_kernel<float, 4096> : nullptr;
+    default: return nullptr;
+  }
+}
+}  // namespace
+
+// lengths with a specialised kernel: FP32 16..4096, FP64 16..2048
+extern "C" int gfft_spec_supported(int dbl, int L) {
+  return (dbl ? spec_fn<double>(L) : spec_fn<float>(L)) != nullptr;
+}
+
+extern "C" int gfft_spec_setup(int dbl, size_t max_smem) {
+  if (dbl) return spec_setup_all<double>(max_smem);
+  int e = spec_setup_all<float>(max_smem);
+  e |= spec_setup_one<float, 4096>(max_smem);
+  return e;
+}
+
+extern "C" int gfft_spec_occupancy(int dbl, int L, int threads, size_t smem) {
+  const void* f = dbl ? spec_fn<double>(L) : spec_fn<float>(L);
+  if (!f) return 0;
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem);
+  return n;
+}
+
+extern "C" int gfft_spec_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                cudaStream_t stream) {
+  const void* f = dbl ? spec_fn<double>(a->L) : spec_fn<float>(a->L);
+  if (!f) return (int)cudaErrorInvalidValue;
+  void* args[] = {(void*)a};
+  return (int)cudaLaunchKernel(f, dim3(grid), dim3(threads), args, smem, stream);
+}

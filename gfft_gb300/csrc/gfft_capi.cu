@@ -24,6 +24,10 @@ extern "C" int gfft_fast_setup(int dbl, size_t max_smem);
 extern "C" int gfft_fast_occupancy(int dbl, int threads, size_t smem);
 extern "C" int gfft_fast_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                 cudaStream_t stream);
+extern "C" int gfft_spec_setup(int dbl, size_t max_smem);
+extern "C" int gfft_spec_occupancy(int dbl, int L, int threads, size_t smem);
+extern "C" int gfft_spec_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                cudaStream_t stream);
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
 
@@ -60,6 +64,7 @@ int setup_device_once(int dbl) {
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (gfft_engine_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_fast_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
+  if (gfft_spec_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (dev < 64) done[dbl][dev] = true;
   return GFFT_OK;
 }
@@ -210,8 +215,11 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
     for (int g = 0; g < h->hp.nglobal; ++g) {
       const GlobalPass& gp = h->hp.gp[g];
-      if (gp.variant != 2) continue;
-      int per = (opts && opts->blocks_per_sm) ? opts->blocks_per_sm : gfft_fast_occupancy(dbl, gp.threads, gp.smem);
+      if (gp.variant < 2) continue;
+      int per = (opts && opts->blocks_per_sm)
+                    ? opts->blocks_per_sm
+                    : (gp.variant == 3 ? gfft_spec_occupancy(dbl, gp.L, gp.threads, gp.smem)
+                                       : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
       if (per < 1) per = 1;
       long long grid = (long long)nsm * per;
       if (grid > gp.ntiles) grid = gp.ntiles;
@@ -364,13 +372,15 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     a.conj = inverse ? 1 : 0;
     a.scale = (inverse && last) ? 1.0 / (double)n : 1.0;
     a.status = h->d_status;
-    if (gp.variant == 2) {
+    if (gp.variant >= 2) {
       a.ntiles = gp.ntiles;
       a.stages = gp.stages;
       a.tile_bytes = gp.tile_bytes;
       a.spin_limit = 1LL << 26;
       a.debug_no_issue = 0;
-      if (gfft_fast_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      const int e = gp.variant == 3 ? gfft_spec_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream)
+                                    : gfft_fast_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream);
+      if (e != 0) return GFFT_E_CUDA;
       continue;
     }
     long long grid = (a.nunits + a.W - 1) / a.W;
@@ -397,7 +407,10 @@ int gfft_selftest_bounded_wait(long long spin_limit, int* status) {
   if (!status) return GFFT_E_NULL_POINTER;
   if (spin_limit < 1) return GFFT_E_INVALID_PLAN;
   gfft_handle h = nullptr;
-  int st = gfft_create(&h, 4096, 1, 0, 1, 0, 1, 64);
+  gfft_plan_opts o;
+  std::memset(&o, 0, sizeof(o));
+  o.kernel_variant = 2;
+  int st = gfft_create_opts(&h, 4096, 1, 0, 1, 0, 1, 64, &o);
   if (st != GFFT_OK) return st;
   const GlobalPass& gp = h->hp.gp[0];
   if (gp.variant != 2) {

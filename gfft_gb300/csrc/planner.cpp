@@ -236,6 +236,8 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       const long long tile = (long long)W * gp.L * esz;
       if (T >= 32 && T % 32 == 0 && T <= 512 && tile % 16 == 0) {
         int S = o.stages > 0 ? o.stages : 2;
+        // keep the block within the opt-in shared memory of one SM
+        while (S > 1 && S * ((tile + 127) & ~127LL) + W * padded(gp.L) * esz + 8 * S > 220 * 1024) --S;
         gp.variant = 2;
         gp.units = W;
         gp.threads = (int)T;
@@ -245,6 +247,20 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         const long long tb_al = (tile + 127) & ~127LL;
         gp.smem = (size_t)(S * tb_al + ((W * padded(gp.L) * esz + 7) & ~7LL) + 8 * S);
       }
+    }
+    // length-specialised variant: default radix order, L in the compiled set
+    const long long TILE = dbl ? 2048 : 4096;
+    bool spec = gp.variant == 2 && (o.variant == 0 || o.variant == 3) && o.units == 0 && o.threads == 0 &&
+                gp.L <= TILE && o.radix_order == 0 && o.max_radix == 16;
+    if (spec) {
+      const long long W = TILE / gp.L;
+      gp.variant = 3;
+      gp.units = (int)W;
+      gp.threads = (int)(TILE / 16);
+      gp.tile_bytes = (int)(TILE * esz);
+      gp.ntiles = (batch + W - 1) / W;
+      const int S = gp.stages;
+      gp.smem = (size_t)(S * TILE * esz + ((W * padded(gp.L) * esz + 7) & ~7LL) + 8 * S);
     }
     Ns *= gp.L;
   }

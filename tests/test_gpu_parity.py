@@ -363,11 +363,14 @@ def test_fast_path_matches_generic_engine(cuda, oracle):
         x = inputs.uniform(55 + n, 2 * n * B).astype(dt)
         ex = oracle.fft_ld(x.astype(np.float64), n, B, 1)
         for tr in (0, 1):
-            fast = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+            spec = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+            fast = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 2})
             gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
             if tr == 0:
+                assert rel(spec, ex) <= tol(n, dbl), (n, rel(spec, ex))
                 assert rel(fast, ex) <= tol(n, dbl), (n, rel(fast, ex))
             assert rel(fast, gen) <= tol(n, dbl), (n, tr, rel(fast, gen))
+            assert rel(spec, gen) <= tol(n, dbl), (n, tr, rel(spec, gen))
         for stages in (1, 2, 3, 4):
             y = run_gpu(cuda, n, vt, 0, 1, x, batch=B, opts={"stages": stages})
             assert rel(y, ex) <= tol(n, dbl), (n, stages)
