@@ -37,10 +37,10 @@ N = 4096
 BATCH = 65536
 WORKLOAD = "fp32 c2c fft N=4096 x batch 65536, out of place"
 
-# DRAM bytes (read + write) of one launch of the engine kernel on this
-# workload, from the ncu capture summarised in
-# profiles/engine_fp32_n4096.md (None until captured).
-NCU_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) of one launch on this workload: the ncu capture
+# summarised in profiles/spec_kernel_fp32_n4096.md measured 1.0248e9 bytes
+# for batch 16384; traffic scales with the transforms processed (x4).
+NCU_TRAFFIC_BYTES = {(4096, 65536): 4 * 1.0248e9}
 
 
 def parse():
@@ -247,7 +247,7 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": NCU_TRAFFIC_BYTES, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": NCU_TRAFFIC_BYTES.get((n, batch)), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": launch_ms}
 
     # end to end through the C ABI host entry point, pinned host buffers
