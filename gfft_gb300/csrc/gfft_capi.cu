@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/gfft_gb300.h"
+#include "handle.h"
 #include "plan.h"
 
 extern "C" int gfft_engine_setup(int dbl, size_t max_smem);
@@ -31,21 +32,6 @@ extern "C" int gfft_spec_launch(int dbl, const EngineArgs* a, unsigned grid, uns
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
 
-struct gfft_plan {
-  HostPlan hp;
-  int vtype = 0;
-  int device = 0;
-  void* d_tab = nullptr;
-  size_t tab_bytes = 0;
-  void* d_ws[2] = {nullptr, nullptr};
-  size_t ws_bytes = 0;
-  // staging buffers for gfft_exec_host, allocated on first use
-  void* d_stage = nullptr;
-  size_t stage_bytes = 0;
-  int* d_status = nullptr;     // device status word of this handle's kernels
-  unsigned grid[GFFT_MAXG] = {0, 0, 0, 0};  // persistent grid of fast-path passes
-  unsigned magic = 0x6FF7B300u;
-};
 
 namespace {
 
