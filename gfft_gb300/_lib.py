@@ -23,7 +23,7 @@ STATUS_NAMES = {
 # every symbol the header declares, checked by the CPU tests
 EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
             "gfft_get_info", "gfft_plan_query", "gfft_get_device_status", "gfft_selftest_bounded_wait",
-            "gfft_version"]
+            "gfft_exec_noalloc", "gfft_version"]
 
 
 class PlanOpts(ctypes.Structure):
@@ -80,6 +80,7 @@ def lib():
         L.gfft_version.restype = ctypes.c_char_p
         L.gfft_get_device_status.argtypes = [vp, ctypes.POINTER(ci)]
         L.gfft_selftest_bounded_wait.argtypes = [ctypes.c_longlong, ctypes.POINTER(ci)]
+        L.gfft_exec_noalloc.argtypes = [u64, ci, ci, u64, vp, vp, vp]
         for name in EXPORTED:
             getattr(L, name).restype = getattr(L, name).restype or ci
         L.gfft_strerror.restype = ctypes.c_char_p

@@ -139,6 +139,35 @@ int gfft_get_device_status(gfft_handle handle, int* status);
  * GFFT_E_TIMEOUT) in *status.  No reference counterpart. */
 int gfft_selftest_bounded_wait(long long spin_limit, int* status);
 
+/* A transform that allocates nothing.  No counterpart in the reference (its
+ * transform objects never touch device memory).
+ *
+ * For callers that cannot call cudaMalloc when they transform: code whose
+ * device memory is fixed at start-up (real-time and embedded pipelines), a
+ * plugin inside a host application that owns every allocation, or a caller
+ * for whom an allocation would synchronise the device at a bad moment.  A
+ * handle from gfft_create allocates its twiddle tables and, for lengths that
+ * need several passes through HBM, a workspace as large as the data; this
+ * entry point keeps both in one fixed device array that the library reserves
+ * on every GPU that loads it, held until the process exits, and plans on the
+ * stack.
+ *
+ * Computes the complex DFT (trans_id 0) or IDFT (1) of `batch` transforms of
+ * length n from src to dst (device pointers; in place when src == dst) on
+ * `stream`.  Limits: n * batch * element size <= 64 MiB (32 MiB when an odd
+ * number of passes runs in place: two workspaces), twiddle tables <= 1 MiB;
+ * larger requests return GFFT_E_TOO_LARGE, real transforms
+ * GFFT_E_INVALID_TRANSFORM.
+ *
+ * The first call on a device looks up the array's address with
+ * cudaGetSymbolAddress (the device must be current); make that first call
+ * before any stream capture.  All calls share the one array and leave their
+ * data in it: nothing needs clearing (each call writes what it reads), but
+ * calls that overlap on the GPU -- on two streams, or from two threads
+ * without ordering -- race on it and must be serialised by the caller. */
+int gfft_exec_noalloc(uint64_t n, int vtype_id, int trans_id, uint64_t batch, const void* src, void* dst,
+                      gfft_stream stream);
+
 /* Library version string. */
 const char* gfft_version(void);
 
