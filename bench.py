@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    p.add_argument("--suite", action="store_true",
+                   help="time every configuration of the workload list (one JSON line each) instead of the headline")
     return p.parse_args()
 
 
@@ -186,10 +188,137 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+SUITE = [
+    # name, n, batch, dtype, trans (0 DFT, 2 RDFT), place, inputs, also time the inverse
+    ("c1 fp64 c2c N=1024 x 4096 in place + ifft", 1024, 4096, "f64", 0, 0, "uniform", True),
+    ("c2 fp32 c2c N=3*2^18 x 8", 3 * 2 ** 18, 8, "f32", 0, 1, "gaussian", False),
+    ("c2 fp64 c2c N=3*2^18 x 8", 3 * 2 ** 18, 8, "f64", 0, 1, "gaussian", False),
+    ("c2 fp32 c2c N=5^8 x 8", 5 ** 8, 8, "f32", 0, 1, "gaussian", False),
+    ("c2 fp64 c2c N=5^8 x 8", 5 ** 8, 8, "f64", 0, 1, "gaussian", False),
+    ("c2 fp32 c2c N=2^10*3^5 x 8", 2 ** 10 * 3 ** 5, 8, "f32", 0, 1, "gaussian", False),
+    ("c2 fp64 c2c N=2^10*3^5 x 8", 2 ** 10 * 3 ** 5, 8, "f64", 0, 1, "gaussian", False),
+    ("c2b fp64 real N_real=2^20 x 16 in place", 2 ** 19, 16, "f64", 2, 0, "uniform", False),
+    ("c3 fp32 c2c N=4096 x 65536", 4096, 65536, "f32", 0, 1, "gaussian", False),
+    ("c3 fp32 c2c N=2^24 x 1", 2 ** 24, 1, "f32", 0, 1, "gaussian", False),
+]
+
+
+def run_suite(args):
+    """Every configuration of the workload list at full size: GFLOP/s, the
+    fraction of the HBM roofline by algorithmic bytes, and an accuracy spot
+    check of one transform against numpy's FP64 FFT."""
+    import numpy as np
+    import torch
+
+    import gfft_gb300
+    from gfft_gb300 import gfft as G
+    from gfft_gb300 import inputs
+    gfft_gb300.build()
+    peak, _ = measured_peaks()
+    for name, n, batch, dt, tr, pl, kind, inv in SUITE:
+        dbl = dt == "f64"
+        tdt = torch.float64 if dbl else torch.float32
+        nel = 2 * n * batch
+        gen = inputs.gaussian if kind == "gaussian" else inputs.uniform
+        xh = gen(0x5EED0000 + n, nel)
+        x = torch.from_numpy(xh).to(tdt).cuda()
+        y = x.clone() if pl == 0 else torch.empty_like(x)
+        vt = G.DOUBLE if dbl else G.FLOAT
+        tt = G.RDFT if tr == 2 else G.DFT
+        place = G.IN_PLACE if pl == 0 else G.OUT_OF_PLACE
+        obj = G.TransformObject(n, vt, tt, 1, G.Serial, place, batch)
+        info = obj.info()
+
+        def step(o=obj):
+            if pl == 0:
+                o.fft(y)
+            else:
+                o.fft(x, y)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        steps = max(5, min(200, int(2e9 / max(nel * 8, 1))))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        esz = 8 if dbl else 4
+        fl = (2.5 * (2 * n) * math.log2(2 * n) if tr == 2 else 5.0 * n * math.log2(n)) * batch
+        alg_bytes = 2 * nel * esz
+        line = {"config": name, "n": n, "batch": batch, "dtype": dt, "ms": ms, "GFLOP/s": fl / ms / 1e6,
+                "GB/s_algorithmic": alg_bytes / ms / 1e6, "frac_hbm": alg_bytes / ms / 1e6 / peak,
+                "passes": info["n_global_passes"], "radices": info["radices"], "variant": info["kernel_variant"],
+                "kernels_per_exec": info["kernels_per_exec"]}
+        if inv:
+            invobj = obj.inverse_object()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(steps):
+                invobj.fft(y)
+            e1.record()
+            torch.cuda.synchronize()
+            line["inverse_ms"] = e0.elapsed_time(e1) / steps
+        # accuracy of one transform (fresh run) against numpy's FP64 FFT
+        xs = torch.from_numpy(xh[:2 * n].copy()).to(tdt).cuda()
+        ys = xs.clone() if pl == 0 else torch.empty_like(xs)
+        one = G.TransformObject(n, vt, tt, 1, G.Serial, place, 1)
+        if pl == 0:
+            one.fft(ys)
+        else:
+            one.fft(xs, ys)
+        got = ys.cpu().numpy().astype(np.float64)
+        src = xs.cpu().numpy().astype(np.float64)
+        if tr == 2:
+            f = np.fft.rfft(src)
+            ref = np.empty(2 * n)
+            ref[0], ref[1] = f[0].real, f[n].real
+            ref[2::2], ref[3::2] = f[1:n].real, f[1:n].imag
+        else:
+            c = np.fft.fft(src[0::2] + 1j * src[1::2])
+            ref = np.empty(2 * n)
+            ref[0::2], ref[1::2] = c.real, c.imag
+        line["rel_l2_vs_numpy_f64"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        line["max_abs_vs_numpy_f64"] = float(np.max(np.abs(got - ref)))
+        if not args.no_cpu_baseline:
+            try:
+                line["cpu_baseline"] = suite_cpu(n, batch, dbl, tr, pl, xh)
+            except Exception as e:
+                line["cpu_baseline"] = {"error": str(e)[:200]}
+        print(json.dumps(line), flush=True)
+        del x, y, obj, one
+        torch.cuda.empty_cache()
+
+
+def suite_cpu(n, batch, dbl, tr, pl, xh):
+    """CPU baseline of one suite configuration: the restatement of the
+    reference (OpenMP over the batch) on a bounded sample."""
+    import numpy as np
+
+    from oracle import pyoracle
+    sample = max(1, min(batch, int(2 ** 22 // n)))
+    x = xh[:2 * n * sample].astype(np.float64 if dbl else np.float32)
+    y = np.empty_like(x)
+    vt = 0 if dbl else 1
+    if tr == 2 and (n & (n - 1)):
+        return {"note": "the reference has no real transform of this length"}
+    t0 = time.perf_counter()
+    pyoracle.gfft_batch(n, sample, vt, tr, pl if tr != 2 else 0, x, y)
+    dt = time.perf_counter() - t0
+    fl = (2.5 * (2 * n) * math.log2(2 * n) if tr == 2 else 5.0 * n * math.log2(n)) * sample
+    return {"GFLOP/s": fl / dt / 1e9, "cores": pyoracle.num_threads(), "kind": "port", "sample_batch": sample}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.suite:
+        run_suite(args)
         return
     import torch
 
