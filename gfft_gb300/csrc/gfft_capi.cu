@@ -156,6 +156,11 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
     return GFFT_E_INVALID_SIZE;
   }
   h->vtype = vtype_id;
+  h->trans_id = trans_id;
+  h->place_id = place_id;
+  h->parall_id = parall_id;
+  h->popts = po;
+  h->has_opts = opts != nullptr;
   int st = setup_device_once(dbl);
   if (st != GFFT_OK) {
     delete h;
@@ -239,6 +244,16 @@ int gfft_destroy(gfft_handle h) {
     if (h->d_ws[i]) cudaFree(h->d_ws[i]);
   if (h->d_stage) cudaFree(h->d_stage);
   if (h->d_status) cudaFree(h->d_status);
+  for (int i = 0; i < 2; ++i)
+    if (h->chunk_plan[i]) gfft_destroy(h->chunk_plan[i]);
+  for (int i = 0; i < 3; ++i)
+    if (h->hstream[i]) cudaStreamDestroy(h->hstream[i]);
+  for (int i = 0; i < GFFT_MAX_CHUNKS; ++i) {
+    if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
+    if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
+  }
+  if (h->ev_user) cudaEventDestroy(h->ev_user);
+  if (h->ev_end) cudaEventDestroy(h->ev_end);
   delete h;
   return GFFT_OK;
 }
@@ -448,6 +463,83 @@ int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
   return gfft_exec_ws(h, src, dst, (cudaStream_t)stream, h->d_ws[0], h->d_ws[1]);
 }
 
+// Pipelined host path: the batch is cut into up to GFFT_MAX_CHUNKS slices;
+// slice i is uploaded on one stream, transformed on a second once its upload
+// is done, and downloaded on a third once its transform is done, so the two
+// copy directions and the kernels overlap.  Returns a status.
+static int exec_host_chunked(gfft_handle h, const void* src, void* dst, cudaStream_t user) {
+  const size_t esz = elem_bytes(h->hp.dbl);
+  const long long n = h->hp.n, batch = h->hp.batch;
+  if (h->n_chunks == 0) {
+    const size_t bytes = (size_t)n * (size_t)batch * esz;
+    long long K = (long long)(bytes / (128ull << 20));
+    if (K < 4) K = 4;
+    if (K > GFFT_MAX_CHUNKS) K = GFFT_MAX_CHUNKS;
+    if (K > batch) K = batch;
+    const long long cb = (batch + K - 1) / K;
+    K = (batch + cb - 1) / cb;
+    const long long last = batch - (K - 1) * cb;
+    gfft_plan_opts o;
+    std::memset(&o, 0, sizeof(o));
+    o.radix_order = h->popts.radix_order;
+    o.max_radix = h->popts.max_radix;
+    o.threads_per_block = h->popts.threads;
+    o.units_per_block = h->popts.units;
+    o.max_pass_len = h->popts.max_pass_len;
+    o.kernel_variant = h->popts.variant;
+    o.stages = h->popts.stages;
+    const gfft_plan_opts* op = h->has_opts ? &o : nullptr;
+    int st = gfft_create_opts(&h->chunk_plan[0], (uint64_t)n, h->vtype, h->trans_id, 1, h->parall_id, h->place_id,
+                              (uint64_t)cb, op);
+    if (st != GFFT_OK) return st;
+    if (last != cb) {
+      st = gfft_create_opts(&h->chunk_plan[1], (uint64_t)n, h->vtype, h->trans_id, 1, h->parall_id, h->place_id,
+                            (uint64_t)last, op);
+      if (st != GFFT_OK) return st;
+    }
+    for (int i = 0; i < 3; ++i)
+      if (cudaStreamCreateWithFlags(&h->hstream[i], cudaStreamNonBlocking) != cudaSuccess) return GFFT_E_CUDA;
+    for (long long i = 0; i < K; ++i)
+      if (cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&h->ev_done[i], cudaEventDisableTiming) != cudaSuccess)
+        return GFFT_E_CUDA;
+    if (cudaEventCreateWithFlags(&h->ev_user, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_end, cudaEventDisableTiming) != cudaSuccess)
+      return GFFT_E_CUDA;
+    h->chunk_batch = cb;
+    h->n_chunks = (int)K;
+  }
+  cudaStream_t sin = h->hstream[0], scomp = h->hstream[1], sout = h->hstream[2];
+  // order after earlier work on the caller's stream
+  if (cudaEventRecord(h->ev_user, user) != cudaSuccess) return GFFT_E_CUDA;
+  for (int i = 0; i < 3; ++i)
+    if (cudaStreamWaitEvent(h->hstream[i], h->ev_user, 0) != cudaSuccess) return GFFT_E_CUDA;
+  const long long cb = h->chunk_batch;
+  for (int i = 0; i < h->n_chunks; ++i) {
+    const long long b0 = (long long)i * cb;
+    const long long nb = (b0 + cb <= batch) ? cb : batch - b0;
+    gfft_plan* sub = (nb == cb) ? h->chunk_plan[0] : h->chunk_plan[1];
+    const size_t off = (size_t)b0 * (size_t)n * esz, len = (size_t)nb * (size_t)n * esz;
+    char* dev = (char*)h->d_stage + off;
+    if (cudaMemcpyAsync(dev, (const char*)src + off, len, cudaMemcpyHostToDevice, sin) != cudaSuccess)
+      return GFFT_E_CUDA;
+    if (cudaEventRecord(h->ev_in[i], sin) != cudaSuccess) return GFFT_E_CUDA;
+    if (cudaStreamWaitEvent(scomp, h->ev_in[i], 0) != cudaSuccess) return GFFT_E_CUDA;
+    int st = gfft_exec_ws(sub, dev, dev, scomp, sub->d_ws[0], sub->d_ws[1]);
+    if (st != GFFT_OK) return st;
+    if (cudaEventRecord(h->ev_done[i], scomp) != cudaSuccess) return GFFT_E_CUDA;
+    if (cudaStreamWaitEvent(sout, h->ev_done[i], 0) != cudaSuccess) return GFFT_E_CUDA;
+    if (cudaMemcpyAsync((char*)dst + off, dev, len, cudaMemcpyDeviceToHost, sout) != cudaSuccess)
+      return GFFT_E_CUDA;
+  }
+  if (cudaEventRecord(h->ev_end, sout) != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaStreamWaitEvent(user, h->ev_end, 0) != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaStreamSynchronize(sout) != cudaSuccess || cudaStreamSynchronize(scomp) != cudaSuccess ||
+      cudaStreamSynchronize(sin) != cudaSuccess)
+    return GFFT_E_CUDA;
+  return GFFT_OK;
+}
+
 int gfft_exec_host(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   if (!src || !dst) return GFFT_E_NULL_POINTER;
@@ -461,6 +553,7 @@ int gfft_exec_host(gfft_handle h, const void* src, void* dst, gfft_stream stream
     h->stage_bytes = bytes;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  if (bytes >= (64ull << 20) && h->hp.batch >= 4) return exec_host_chunked(h, src, dst, s);
   if (cudaMemcpyAsync(h->d_stage, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return GFFT_E_CUDA;
   int st = gfft_exec_ws(h, h->d_stage, h->d_stage, s, h->d_ws[0], h->d_ws[1]);
   if (st != GFFT_OK) return st;
