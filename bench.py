@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    p.add_argument("--only", default="", help="with --suite: run the configurations whose name contains this")
     p.add_argument("--suite", action="store_true",
                    help="time every configuration of the workload list (one JSON line each) instead of the headline")
     return p.parse_args()
@@ -216,6 +217,8 @@ def run_suite(args):
     gfft_gb300.build()
     peak, _ = measured_peaks()
     for name, n, batch, dt, tr, pl, kind, inv in SUITE:
+        if args.only and args.only not in name:
+            continue
         dbl = dt == "f64"
         tdt = torch.float64 if dbl else torch.float32
         nel = 2 * n * batch

@@ -34,14 +34,14 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
   const int nb = L / R;
   const int total = a.W * nb;
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
-    const int lane = i / nb;
+    const int lane = (int)fdiv((unsigned)i, p.fd_nb);
     const int j = i - lane * nb;
     const V* s = src + lane * a.Lp;
     V* d = dst + lane * a.Lp;
     V v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = s[pad<T>(j + r * nb)];
-    const int k = j % p.Ns;
+    const int k = j - (int)fdiv((unsigned)j, p.fd_ns) * p.Ns;
     if (p.Ns > 1) {
       const V* t = tw + p.tw + k;
 #pragma unroll
@@ -84,13 +84,13 @@ __device__ void block_pass_generic(const typename Vec<T>::t* __restrict__ src, t
   }
 }
 
+// W_N^m = lo[m mod B] * hi[m / B], B a power of two
 template <typename T>
-__device__ __forceinline__ typename Vec<T>::t global_twiddle(const EngineArgs& a, long long m) {
+__device__ __forceinline__ typename Vec<T>::t global_twiddle(const EngineArgs& a, long long m, int lgB) {
   typedef typename Vec<T>::t V;
   const V* lo = (const V*)a.gtw_lo;
   const V* hi = (const V*)a.gtw_hi;
-  const long long q = m / a.gB;
-  return cmul(__ldg(lo + (m - q * a.gB)), __ldg(hi + q));
+  return cmul(__ldg(lo + (m & (a.gB - 1))), __ldg(hi + (m >> lgB)));
 }
 
 // global -> shared, with the conjugation of the inverse, the inter-pass
@@ -107,7 +107,7 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
     const V* rtw = (const V*)a.rtw;
     const int half = L / 2 + 1;
     for (int i = threadIdx.x; i < a.W * half; i += blockDim.x) {
-      const int lane = i / half;
+      const int lane = (int)fdiv((unsigned)i, a.fd_half);
       const int q = i - lane * half;
       const long long u = u0 + lane;
       V* b = buf + lane * a.Lp;
@@ -144,31 +144,35 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
     const V* tile = in + u0 * L;
     const long long lim = (a.nunits - u0) * L;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
-      const int lane = i / L;
+      const int lane = (int)fdiv((unsigned)i, a.fd_L);
       const int s = i - lane * L;
       V v = (i < lim) ? tile[i] : mk<V>(0, 0);
       if (a.conj) v = cconj(v);
       buf[lane * a.Lp + pad<T>(s)] = v;
     }
   } else {
+    // lane units: the block's threads are a whole number of W-groups, so
+    // each thread keeps one lane and walks its samples
     const int W = a.W;
-    const long long mstep = a.N / (a.gNs * L);
-    for (int i = threadIdx.x; i < total; i += blockDim.x) {
-      const int lane = i % W;
-      const int s = i / W;
-      const long long u = u0 + lane;
-      V v = mk<V>(0, 0);
-      if (u < a.nunits) {
-        const long long t = u / a.stride;
-        const long long b = u - t * a.stride;
-        v = in[t * a.N + b + (long long)s * a.stride];
-        if (a.conj) v = cconj(v);
-        if (a.gNs > 1) {
-          const long long k = b % a.gNs;
-          v = cmul(v, global_twiddle<T>(a, (k * s) * mstep));
-        }
-      }
-      buf[lane * a.Lp + pad<T>(s)] = v;
+    const int lane = threadIdx.x % W;
+    const int sstep = blockDim.x / W;
+    const long long u = u0 + lane;
+    V* bl = buf + lane * a.Lp;
+    if (u >= a.nunits) {
+      for (int s = threadIdx.x / W; s < L; s += sstep) bl[pad<T>(s)] = mk<V>(0, 0);
+      return;
+    }
+    const long long t = u / a.stride;
+    const long long b = u - t * a.stride;
+    const long long k = b % a.gNs;
+    const long long kstep = k * (a.N / (a.gNs * L));  // twiddle exponent per sample
+    const int lgB = 63 - __clzll(a.gB);
+    const V* src = in + t * a.N + b;
+    for (int s = threadIdx.x / W; s < L; s += sstep) {
+      V v = src[(long long)s * a.stride];
+      if (a.conj) v = cconj(v);
+      if (kstep) v = cmul(v, global_twiddle<T>(a, kstep * s, lgB));
+      bl[pad<T>(s)] = v;
     }
   }
 }
@@ -186,7 +190,7 @@ __device__ __forceinline__ void store_tile(const EngineArgs& a, const typename V
     const V* rtw = (const V*)a.rtw;
     const int half = L / 2 + 1;
     for (int i = threadIdx.x; i < a.W * half; i += blockDim.x) {
-      const int lane = i / half;
+      const int lane = (int)fdiv((unsigned)i, a.fd_half);
       const int q = i - lane * half;
       const long long u = u0 + lane;
       if (u >= a.nunits) continue;
@@ -219,7 +223,7 @@ __device__ __forceinline__ void store_tile(const EngineArgs& a, const typename V
     const long long lim = (a.nunits - u0) * L;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
       if (i >= lim) break;
-      const int lane = i / L;
+      const int lane = (int)fdiv((unsigned)i, a.fd_L);
       const int s = i - lane * L;
       V v = buf[lane * a.Lp + pad<T>(s)];
       if (a.conj) v = cconj(v);
@@ -227,17 +231,19 @@ __device__ __forceinline__ void store_tile(const EngineArgs& a, const typename V
     }
   } else {
     const int W = a.W;
-    for (int i = threadIdx.x; i < total; i += blockDim.x) {
-      const int lane = i % W;
-      const int s = i / W;
-      const long long u = u0 + lane;
-      if (u >= a.nunits) continue;
-      const long long t = u / a.stride;
-      const long long b = u - t * a.stride;
-      const long long k = b % a.gNs;
-      V v = buf[lane * a.Lp + pad<T>(s)];
+    const int lane = threadIdx.x % W;
+    const int sstep = blockDim.x / W;
+    const long long u = u0 + lane;
+    if (u >= a.nunits) return;
+    const long long t = u / a.stride;
+    const long long b = u - t * a.stride;
+    const long long k = b % a.gNs;
+    V* dstp = out + t * a.N + (b - k) * L + k;
+    const V* bl = buf + lane * a.Lp;
+    for (int s = threadIdx.x / W; s < L; s += sstep) {
+      V v = bl[pad<T>(s)];
       if (a.conj) v = cconj(v);
-      out[t * a.N + (b - k) * L + k + (long long)s * a.gNs] = cscale(v, sc);
+      dstp[(long long)s * a.gNs] = cscale(v, sc);
     }
   }
 }

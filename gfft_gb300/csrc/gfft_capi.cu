@@ -363,7 +363,13 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     a.W = gp.units;
     a.mode = gp.mode;
     a.npass = gp.npass;
-    for (int i = 0; i < gp.npass; ++i) a.pass[i] = gp.pass[i];
+    for (int i = 0; i < gp.npass; ++i) {
+      a.pass[i] = gp.pass[i];
+      a.pass[i].fd_nb = make_fastdiv((unsigned)(gp.L / gp.pass[i].R));
+      a.pass[i].fd_ns = make_fastdiv((unsigned)gp.pass[i].Ns);
+    }
+    a.fd_L = make_fastdiv((unsigned)gp.L);
+    a.fd_half = make_fastdiv((unsigned)(gp.L / 2 + 1));
     const bool last = (g == p.nglobal - 1);
     a.real = p.real_fused ? ((p.trans == 2) ? 1 : 2) : 0;
     // The inverse runs as conj(FFT(conj x)) / N.  Every pass conjugates on

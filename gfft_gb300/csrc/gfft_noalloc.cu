@@ -189,7 +189,9 @@ bool plan(HostPlan& hp, long long n, long long batch, int dbl, int trans, int pl
       gp.units = (int)W;
     } else {
       const long long stride = n / gp.L;
-      gp.units = (int)(stride < lane_w ? stride : lane_w);
+      long long W = 1;
+      while (W * 2 <= (stride < lane_w ? stride : lane_w)) W *= 2;
+      gp.units = (int)W;
     }
     long long el = (long long)gp.units * gp.L / 16;
     gp.threads = round32(el < 64 ? 64 : (el > 512 ? 512 : el));

@@ -20,11 +20,43 @@
 #define GFFT_MAXP 16     // in-block passes
 #define GFFT_MAXG 4      // global passes
 
+// Unsigned division by a run-time invariant d via multiply and shift
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, round-up method): for d > 1 with
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1 and t = umulhi(x, m),
+// x / d = (t + ((x - t) >> 1)) >> (l - 1) for every 32-bit x.
+struct FastDiv {
+  unsigned d, m, l;
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  f.d = d;
+  if (d <= 1) {
+    f.m = 0;
+    f.l = 0;
+    return f;
+  }
+  unsigned l = 0;
+  while ((1ull << l) < d) ++l;
+  f.l = l;
+  f.m = (unsigned)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+  return f;
+}
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned fdiv(unsigned x, const FastDiv& f) {
+  if (f.d <= 1) return x;
+  const unsigned t = __umulhi(x, f.m);
+  return (t + ((x - t) >> 1)) >> (f.l - 1);
+}
+#endif
+
 struct BlockPass {
   int R;    // radix
   int Ns;   // product of the radices before this pass
   int tw;   // offset (complex elements) of this pass's twiddles in the table
   int gen;  // generic odd prime: offset of its W_R^m table (else -1)
+  FastDiv fd_nb;  // L / R
+  FastDiv fd_ns;  // Ns
 };
 
 // Arguments of one launch of the engine kernel (passed by value).
@@ -56,6 +88,8 @@ struct EngineArgs {
   int tile_bytes;     // bytes of one tile (multiple of 16)
   long long spin_limit;  // bound on every mbarrier wait (try_wait iterations)
   int debug_no_issue; // test hook: never issue the copies, so the first wait runs out
+  FastDiv fd_L;       // L
+  FastDiv fd_half;    // L/2 + 1 (real pre/post pass)
   BlockPass pass[GFFT_MAXP];
 };
 

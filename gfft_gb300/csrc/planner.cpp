@@ -162,7 +162,8 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   // largest single-pass length: two padded buffers of one transform
   long long cap1 = dbl ? 4096 : 8192;
   if (o.max_pass_len > 0) cap1 = std::min<long long>(cap1, o.max_pass_len);
-  const int lane_w = o.units > 0 ? o.units : (dbl ? 4 : 8);  // 64-byte rows
+  int lane_w = o.units > 0 ? o.units : (dbl ? 4 : 8);  // 64-byte rows
+  if (lane_w > 32) lane_w = 32;
   long long capL = 1;
   while (2 * lane_w * padded(capL * 2) * esz <= smem_budget) capL *= 2;
   if (o.max_pass_len > 0) capL = std::min<long long>(capL, o.max_pass_len);
@@ -213,8 +214,11 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       while (W > 1 && 2LL * W * padded(gp.L) * esz > smem_budget) --W;
       gp.units = W;
     } else {
+      // lane units: a power of two that divides the block (each thread keeps one lane)
       long long stride = n / gp.L;
-      gp.units = (int)std::min<long long>(lane_w, stride);
+      long long W = 1;
+      while (W * 2 <= std::min<long long>(lane_w, stride)) W *= 2;
+      gp.units = (int)W;
     }
     long long elems = (long long)gp.units * gp.L;
     int thr = o.threads > 0 ? o.threads : round32(std::min<long long>(512, std::max<long long>(64, elems / 16)));
