@@ -143,12 +143,23 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
   if (a.mode == 0) {
     const V* tile = in + u0 * L;
     const long long lim = (a.nunits - u0) * L;
-    for (int i = threadIdx.x; i < total; i += blockDim.x) {
-      const int lane = (int)fdiv((unsigned)i, a.fd_L);
-      const int s = i - lane * L;
-      V v = (i < lim) ? tile[i] : mk<V>(0, 0);
-      if (a.conj) v = cconj(v);
-      buf[lane * a.Lp + pad<T>(s)] = v;
+    // eight loads in flight per thread before their shared-memory stores
+    const int step = blockDim.x;
+    for (int i0 = threadIdx.x; i0 < total; i0 += 8 * step) {
+      V v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int i = i0 + q * step;
+        v[q] = (i < total && i < lim) ? tile[i] : mk<V>(0, 0);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int i = i0 + q * step;
+        if (i >= total) break;
+        const int lane = (int)fdiv((unsigned)i, a.fd_L);
+        const int s = i - lane * L;
+        buf[lane * a.Lp + pad<T>(s)] = a.conj ? cconj(v[q]) : v[q];
+      }
     }
   } else {
     // lane units: the block's threads are a whole number of W-groups, so
@@ -168,11 +179,21 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
     const long long kstep = k * (a.N / (a.gNs * L));  // twiddle exponent per sample
     const int lgB = 63 - __clzll(a.gB);
     const V* src = in + t * a.N + b;
-    for (int s = threadIdx.x / W; s < L; s += sstep) {
-      V v = src[(long long)s * a.stride];
-      if (a.conj) v = cconj(v);
-      if (kstep) v = cmul(v, global_twiddle<T>(a, kstep * s, lgB));
-      bl[pad<T>(s)] = v;
+    for (int s0 = threadIdx.x / W; s0 < L; s0 += 8 * sstep) {
+      V v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int s = s0 + q * sstep;
+        if (s < L) v[q] = src[(long long)s * a.stride];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int s = s0 + q * sstep;
+        if (s >= L) break;
+        V x = a.conj ? cconj(v[q]) : v[q];
+        if (kstep) x = cmul(x, global_twiddle<T>(a, kstep * s, lgB));
+        bl[pad<T>(s)] = x;
+      }
     }
   }
 }
