@@ -5,11 +5,11 @@ the compute runs in the in-tree CUDA library ``libgfft_gb300.so`` through its
 C ABI (include/gfft_gb300.h).  There is no CPU fallback.
 """
 from .gfft import (COMPLEX_DOUBLE, COMPLEX_FLOAT, DFT, DOUBLE, FLOAT, IDFT, IN_PLACE, IRDFT, OUT_OF_PLACE, RDFT,
-                   GenerateTransform, OpenMP, ParallelizationGroup, PlaceGroup, Serial, Transform,
+                   GenerateTransform, OpenMP, ParallelizationGroup, PlaceGroup, RaggedBatch, Serial, Transform,
                    TransformFactoryError, TransformObject, TransformTypeGroup, ValueTypeGroup)
 from ._lib import GfftError, build, lib
 
 __all__ = ["COMPLEX_DOUBLE", "COMPLEX_FLOAT", "DFT", "DOUBLE", "FLOAT", "IDFT", "IN_PLACE", "IRDFT", "OUT_OF_PLACE",
-           "RDFT", "GenerateTransform", "OpenMP", "ParallelizationGroup", "PlaceGroup", "Serial", "Transform",
+           "RDFT", "RaggedBatch", "GenerateTransform", "OpenMP", "ParallelizationGroup", "PlaceGroup", "Serial", "Transform",
            "TransformFactoryError", "TransformObject", "TransformTypeGroup", "ValueTypeGroup", "GfftError", "build",
            "lib"]

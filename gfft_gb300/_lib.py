@@ -23,7 +23,8 @@ STATUS_NAMES = {
 # every symbol the header declares, checked by the CPU tests
 EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
             "gfft_get_info", "gfft_plan_query", "gfft_get_device_status", "gfft_selftest_bounded_wait",
-            "gfft_exec_noalloc", "gfft_version"]
+            "gfft_exec_noalloc", "gfft_ragged_create", "gfft_ragged_exec", "gfft_ragged_get_info",
+            "gfft_ragged_get_status", "gfft_ragged_destroy", "gfft_version"]
 
 
 class PlanOpts(ctypes.Structure):
@@ -81,6 +82,12 @@ def lib():
         L.gfft_get_device_status.argtypes = [vp, ctypes.POINTER(ci)]
         L.gfft_selftest_bounded_wait.argtypes = [ctypes.c_longlong, ctypes.POINTER(ci)]
         L.gfft_exec_noalloc.argtypes = [u64, ci, ci, u64, vp, vp, vp]
+        L.gfft_ragged_create.argtypes = [ctypes.POINTER(vp), u64, ctypes.POINTER(u64), ci, ci]
+        L.gfft_ragged_exec.argtypes = [vp, vp, vp, vp]
+        L.gfft_ragged_get_info.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(ci),
+                                           ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_uint)]
+        L.gfft_ragged_get_status.argtypes = [vp, ctypes.POINTER(ci)]
+        L.gfft_ragged_destroy.argtypes = [vp]
         for name in EXPORTED:
             getattr(L, name).restype = getattr(L, name).restype or ci
         L.gfft_strerror.restype = ctypes.c_char_p

@@ -1,0 +1,486 @@
+// Ragged batches: transforms of many different lengths in ONE persistent
+// launch driven by a device work queue, replayed from a CUDA graph.
+//
+// The reference's only batching is its OpenMP loop inside one transform
+// (ParallLoop, src/gfftomp.h:41-189); a caller with many lengths builds one
+// object per length (GenerateTransform over an NList, src/gfftgen.h:189-231)
+// and runs them one after another.  Here every length gets a plan (the same
+// planner as gfft_create, with a tighter shared-memory budget so that three
+// blocks share an SM), and the whole set becomes a list of work items
+// (plan, global pass, tile):
+//
+//   - a single-pass length contributes groups of up to W whole transforms
+//     (lanes gathered from their own offsets);
+//   - a multi-pass length contributes, per transform and per global pass,
+//     tiles of W columns; the tiles of pass g+1 of a transform may start only
+//     when all of its pass-g tiles are done (a per-(transform, pass) counter).
+//
+// Items are ordered largest first (the first passes of the long transforms,
+// then the single-pass groups by length, then the later passes), and
+// persistent blocks take them from a global queue head with atomicAdd.  A
+// later-pass item is taken only after every earlier-pass item was taken by a
+// running block, so its wait always ends; the wait is bounded anyway
+// (RaggedArgs::spin_limit, then GFFT_E_TIMEOUT in the status word).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/gfft_gb300.h"
+#include "engine.cuh"
+#include "plan.h"
+
+namespace gfft {
+
+template <typename T>
+__global__ void __launch_bounds__(256) ragged_kernel(const __grid_constant__ RaggedArgs ra) {
+  typedef typename Vec<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ EngineArgs ea;
+  __shared__ long long item_s;
+  __shared__ int abort_s;
+  V* b0 = reinterpret_cast<V*>(smem_raw);
+  V* b1 = b0 + ra.lanes_max;
+  const V* tab = (const V*)ra.tab;
+  while (true) {
+    if (threadIdx.x == 0) {
+      item_s = atomicAdd(ra.head, 1);
+      abort_s = 0;
+    }
+    __syncthreads();
+    const long long it = item_s;
+    if (it >= ra.nitems) return;
+    if (threadIdx.x == 0) {
+      const RaggedItem item = ra.items[it];
+      const RaggedPlan& pl = ra.plans[item.plan];
+      const int g = item.pass;
+      if (g > 0) {  // wait for every tile of the previous pass of this transform
+        volatile int* d = ra.done + (long long)item.transform * GFFT_MAXG + (g - 1);
+        long long i = 0;
+        while (*d < pl.tiles[g - 1] && i < ra.spin_limit) {
+          __nanosleep(64);
+          ++i;
+        }
+        if (*d < pl.tiles[g - 1]) {
+          atomicExch(ra.status, 13 /* GFFT_E_TIMEOUT */);
+          abort_s = 1;
+        }
+        __threadfence();
+      }
+      const int L = pl.L[g];
+      const int ps = sizeof(T) == 8 ? 3 : 4;
+      ea.L = L;
+      ea.Lp = L + (L >> ps) + 1;
+      ea.pad_shift = ps;
+      ea.N = pl.n;
+      ea.npass = pl.npass[g];
+      for (int i = 0; i < ea.npass; ++i) {
+        ea.pass[i] = pl.pass[g][i];
+        ea.pass[i].fd_nb = make_fastdiv((unsigned)(L / ea.pass[i].R));
+        ea.pass[i].fd_ns = make_fastdiv((unsigned)ea.pass[i].Ns);
+      }
+      ea.fd_L = make_fastdiv((unsigned)L);
+      ea.tw = tab + pl.tab;
+      ea.gtw_lo = tab + pl.tab + pl.gtw_lo;
+      ea.gtw_hi = tab + pl.tab + pl.gtw_hi;
+      ea.gB = pl.gB;
+      ea.conj = ra.conj;
+      ea.real = 0;
+      const bool last = (g == pl.nglobal - 1);
+      ea.scale = (ra.conj && last) ? 1.0 / (double)pl.n : 1.0;
+      ea.ldcg = g > 0;
+      if (pl.nglobal == 1) {
+        ea.mode = 2;
+        ea.in = ra.in;
+        ea.out = ra.out;
+        ea.lane_off = ra.lane_off + item.group;
+        ea.W = item.count;
+        ea.nunits = item.count;
+        ea.stride = 1;
+        ea.gNs = 1;
+      } else {
+        // buffer chain: 2 passes in -> ws -> out; 3 passes in -> ws -> ws2 -> out
+        const long long off = ra.offset[item.transform];
+        const V* bufs_in[3] = {(const V*)ra.in, (const V*)ra.ws, (const V*)ra.ws + ra.ws2_off};
+        V* bufs_out[3] = {(V*)ra.ws, (V*)ra.ws + ra.ws2_off, (V*)ra.out};
+        const V* src = bufs_in[g] + off;
+        V* dst = last ? (V*)ra.out + off : bufs_out[g] + off;
+        ea.mode = 1;
+        ea.in = src;
+        ea.out = dst;
+        ea.W = pl.W[g];
+        ea.stride = pl.n / L;
+        ea.nunits = ea.stride;
+        ea.gNs = pl.Ns[g];
+      }
+      item_s = (pl.nglobal == 1) ? 0 : item.unit0;
+    }
+    __syncthreads();
+    if (abort_s) return;
+    const long long u0 = item_s;
+    load_tile<T>(ea, b0, u0);
+    __syncthreads();
+    V* src = b0;
+    V* dst = b1;
+    for (int p = 0; p < ea.npass; ++p) {
+      const BlockPass bp = ea.pass[p];
+      switch (bp.R) {
+        case 16: block_pass<T, 16>(src, dst, ea, bp, (const V*)ea.tw); break;
+        case 8: block_pass<T, 8>(src, dst, ea, bp, (const V*)ea.tw); break;
+        case 4: block_pass<T, 4>(src, dst, ea, bp, (const V*)ea.tw); break;
+        case 2: block_pass<T, 2>(src, dst, ea, bp, (const V*)ea.tw); break;
+        case 3: block_pass<T, 3>(src, dst, ea, bp, (const V*)ea.tw); break;
+        case 5: block_pass<T, 5>(src, dst, ea, bp, (const V*)ea.tw); break;
+        case 7: block_pass<T, 7>(src, dst, ea, bp, (const V*)ea.tw); break;
+        default: block_pass_generic<T>(src, dst, ea, bp, (const V*)ea.tw); break;
+      }
+      __syncthreads();
+      V* t = src;
+      src = dst;
+      dst = t;
+    }
+    store_tile<T>(ea, src, u0);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const RaggedItem& item = ra.items[it];
+      const RaggedPlan& pl = ra.plans[item.plan];
+      if (pl.nglobal > 1 && item.pass < pl.nglobal - 1)
+        atomicAdd(ra.done + (long long)item.transform * GFFT_MAXG + item.pass, 1);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace gfft
+
+struct gfft_ragged {
+  int dbl = 0, inverse = 0;
+  long long count = 0, total = 0;
+  int nplans = 0;
+  long long nitems = 0;
+  void* d_tab = nullptr;
+  RaggedPlan* d_plans = nullptr;
+  RaggedItem* d_items = nullptr;
+  long long* d_lane_off = nullptr;
+  long long* d_offset = nullptr;
+  int* d_done = nullptr;
+  int* d_head = nullptr;
+  int* d_status = nullptr;
+  void* d_ws = nullptr;
+  long long ws2_off = 0;
+  int lanes_max = 0;
+  unsigned grid = 0, threads = 256;
+  size_t smem = 0;
+  size_t done_bytes = 0;
+  // the captured launch sequence and the pointers it was captured with
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  const void* g_src = nullptr;
+  void* g_dst = nullptr;
+  int max_passes = 1;
+  unsigned magic = 0x6A66ED00u;
+};
+
+namespace {
+
+void free_ragged(gfft_ragged* r) {
+  if (!r) return;
+  if (r->gexec) cudaGraphExecDestroy(r->gexec);
+  if (r->graph) cudaGraphDestroy(r->graph);
+  if (r->cap_stream) cudaStreamDestroy(r->cap_stream);
+  void* ps[] = {r->d_tab, r->d_plans, r->d_items, r->d_lane_off, r->d_offset, r->d_done, r->d_head, r->d_status,
+                r->d_ws};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  delete r;
+}
+
+template <typename T>
+int upload(void** dst, const std::vector<T>& v) {
+  size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
+  if (cudaMalloc(dst, bytes) != cudaSuccess) {
+    *dst = nullptr;
+    return GFFT_E_ALLOC;
+  }
+  if (!v.empty() && cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    return GFFT_E_CUDA;
+  return GFFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* sizes, int vtype_id, int trans_id) {
+  if (!handle || !sizes) return GFFT_E_NULL_POINTER;
+  *handle = nullptr;
+  if (count == 0 || count > (1ULL << 31)) return GFFT_E_INVALID_SIZE;
+  if (vtype_id < 0 || vtype_id > 3) return GFFT_E_INVALID_TYPE;
+  if (trans_id != 0 && trans_id != 1) return GFFT_E_INVALID_TRANSFORM;
+  gfft_ragged* r = new (std::nothrow) gfft_ragged();
+  if (!r) return GFFT_E_ALLOC;
+  r->dbl = (vtype_id == 0 || vtype_id == 2) ? 1 : 0;
+  r->inverse = trans_id == 1;
+  r->count = (long long)count;
+  const int esz = r->dbl ? 16 : 8;
+  const int ps = r->dbl ? 3 : 4;
+  // distinct lengths, their plans and tables
+  std::vector<long long> offs(count);
+  std::vector<long long> distinct;
+  long long total = 0;
+  for (uint64_t i = 0; i < count; ++i) {
+    if (sizes[i] == 0) {
+      free_ragged(r);
+      return GFFT_E_INVALID_SIZE;
+    }
+    offs[i] = total;
+    total += (long long)sizes[i];
+    distinct.push_back((long long)sizes[i]);
+  }
+  r->total = total;
+  std::sort(distinct.begin(), distinct.end());
+  distinct.erase(std::unique(distinct.begin(), distinct.end()), distinct.end());
+  PlanOpts po;
+  po.max_single = r->dbl ? 2048 : 4096;
+  po.smem_budget = 72 * 1024;
+  po.variant = 1;
+  std::vector<RaggedPlan> plans(distinct.size());
+  std::vector<double> tab;
+  int lanes_max = 0;
+  for (size_t d = 0; d < distinct.size(); ++d) {
+    HostPlan hp;
+    if (gfft_plan_build(hp, distinct[d], 1, r->dbl, trans_id, 1, po) != 0 || hp.nglobal > 3) {
+      free_ragged(r);
+      return GFFT_E_INVALID_SIZE;
+    }
+    RaggedPlan& rp = plans[d];
+    std::memset(&rp, 0, sizeof(rp));
+    rp.n = distinct[d];
+    rp.nglobal = hp.nglobal;
+    r->max_passes = std::max(r->max_passes, hp.nglobal);
+    for (int g = 0; g < hp.nglobal; ++g) {
+      const GlobalPass& gp = hp.gp[g];
+      rp.L[g] = gp.L;
+      rp.npass[g] = gp.npass;
+      rp.Ns[g] = gp.Ns;
+      for (int i = 0; i < gp.npass; ++i) rp.pass[g][i] = gp.pass[i];
+      if (hp.nglobal == 1) {
+        // groups of whole transforms: about 4096 (FP32) / 2048 (FP64) points
+        int W = std::max<int>(1, (r->dbl ? 2048 : 4096) / gp.L);
+        while (W > 1 && 2LL * W * (gp.L + (gp.L >> ps) + 1) * esz > po.smem_budget) --W;
+        rp.W[g] = W;
+      } else {
+        rp.W[g] = gp.units;
+        rp.tiles[g] = (int)((distinct[d] / gp.L + gp.units - 1) / gp.units);
+      }
+      lanes_max = std::max<int>(lanes_max, rp.W[g] * (gp.L + (gp.L >> ps) + 1));
+    }
+    rp.tab = (long long)(tab.size() / 2);
+    rp.gtw_lo = (long long)hp.gtw_lo_off;
+    rp.gtw_hi = (long long)hp.gtw_hi_off;
+    rp.gB = (long long)hp.gtw_B;
+    std::vector<double> t(2 * std::max<size_t>(hp.table_count, 1), 0.0);
+    gfft_plan_tables(hp, t.data());
+    tab.insert(tab.end(), t.begin(), t.end());
+  }
+  r->nplans = (int)plans.size();
+  r->lanes_max = lanes_max;
+  // work items, largest first
+  std::vector<std::vector<long long>> members(distinct.size());
+  for (uint64_t i = 0; i < count; ++i) {
+    size_t d = std::lower_bound(distinct.begin(), distinct.end(), (long long)sizes[i]) - distinct.begin();
+    members[d].push_back((long long)i);
+  }
+  std::vector<RaggedItem> items;
+  std::vector<long long> lane_off;
+  auto add_multi = [&](int g) {
+    for (size_t dd = distinct.size(); dd-- > 0;) {
+      const RaggedPlan& rp = plans[dd];
+      if (rp.nglobal <= g || rp.nglobal == 1) continue;
+      const long long stride = rp.n / rp.L[g];
+      for (long long t : members[dd])
+        for (int k = 0; k < rp.tiles[g]; ++k) {
+          RaggedItem it;
+          it.plan = (int)dd;
+          it.pass = g;
+          it.transform = (int)t;
+          it.unit0 = (long long)k * rp.W[g];
+          it.count = (int)std::min<long long>(rp.W[g], stride - it.unit0);
+          it.group = 0;
+          items.push_back(it);
+        }
+    }
+  };
+  add_multi(0);
+  for (size_t dd = distinct.size(); dd-- > 0;) {
+    const RaggedPlan& rp = plans[dd];
+    if (rp.nglobal != 1) continue;
+    const std::vector<long long>& m = members[dd];
+    for (size_t k = 0; k < m.size(); k += rp.W[0]) {
+      RaggedItem it;
+      it.plan = (int)dd;
+      it.pass = 0;
+      it.transform = (int)m[k];
+      it.unit0 = 0;
+      it.count = (int)std::min<size_t>(rp.W[0], m.size() - k);
+      it.group = (long long)lane_off.size();
+      for (int j = 0; j < it.count; ++j) lane_off.push_back(offs[m[k + j]]);
+      items.push_back(it);
+    }
+  }
+  add_multi(1);
+  add_multi(2);
+  r->nitems = (long long)items.size();
+  // device buffers
+  int st = GFFT_OK;
+  if (r->dbl) {
+    st = upload(&r->d_tab, tab);
+  } else {
+    std::vector<float> f(tab.begin(), tab.end());
+    st = upload(&r->d_tab, f);
+  }
+  if (st == GFFT_OK) st = upload((void**)&r->d_plans, plans);
+  if (st == GFFT_OK) st = upload((void**)&r->d_items, items);
+  if (st == GFFT_OK) st = upload((void**)&r->d_lane_off, lane_off);
+  if (st == GFFT_OK) st = upload((void**)&r->d_offset, offs);
+  r->done_bytes = (size_t)count * GFFT_MAXG * sizeof(int);
+  if (st == GFFT_OK && cudaMalloc((void**)&r->d_done, r->done_bytes) != cudaSuccess) st = GFFT_E_ALLOC;
+  if (st == GFFT_OK && cudaMalloc((void**)&r->d_head, 256) != cudaSuccess) st = GFFT_E_ALLOC;
+  if (st == GFFT_OK && (cudaMalloc((void**)&r->d_status, 256) != cudaSuccess ||
+                        cudaMemset(r->d_status, 0, 256) != cudaSuccess))
+    st = GFFT_E_ALLOC;
+  if (st == GFFT_OK && r->max_passes > 1) {
+    r->ws2_off = r->max_passes > 2 ? total : 0;
+    const size_t wsb = (size_t)total * esz * (r->max_passes > 2 ? 2 : 1);
+    if (cudaMalloc(&r->d_ws, wsb) != cudaSuccess) st = GFFT_E_ALLOC;
+  }
+  if (st == GFFT_OK && cudaStreamCreateWithFlags(&r->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+    st = GFFT_E_CUDA;
+  if (st != GFFT_OK) {
+    free_ragged(r);
+    return st;
+  }
+  // persistent grid: every block resident
+  r->smem = (size_t)2 * lanes_max * esz;
+  int maxopt = 0, nsm = 0, dev = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t ce = r->dbl ? cudaFuncSetAttribute(gfft::ragged_kernel<double>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt)
+                          : cudaFuncSetAttribute(gfft::ragged_kernel<float>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+  if (ce != cudaSuccess) {
+    free_ragged(r);
+    return GFFT_E_CUDA;
+  }
+  if (r->dbl)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gfft::ragged_kernel<double>, r->threads, r->smem);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gfft::ragged_kernel<float>, r->threads, r->smem);
+  if (per < 1) {
+    free_ragged(r);
+    return GFFT_E_INVALID_SIZE;
+  }
+  r->grid = (unsigned)std::min<long long>((long long)nsm * per, r->nitems);
+  *handle = r;
+  return GFFT_OK;
+}
+
+static int ragged_launch(gfft_ragged* r, const void* src, void* dst, cudaStream_t s) {
+  if (cudaMemsetAsync(r->d_done, 0, r->done_bytes, s) != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaMemsetAsync(r->d_head, 0, sizeof(int), s) != cudaSuccess) return GFFT_E_CUDA;
+  RaggedArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.in = src;
+  a.out = dst;
+  a.ws = r->d_ws;
+  a.ws2_off = r->ws2_off;
+  a.tab = r->d_tab;
+  a.plans = r->d_plans;
+  a.items = r->d_items;
+  a.lane_off = r->d_lane_off;
+  a.offset = r->d_offset;
+  a.done = r->d_done;
+  a.head = r->d_head;
+  a.status = r->d_status;
+  a.nitems = r->nitems;
+  a.spin_limit = 1LL << 24;
+  a.conj = r->inverse;
+  a.lanes_max = r->lanes_max;
+  if (r->dbl)
+    gfft::ragged_kernel<double><<<r->grid, r->threads, r->smem, s>>>(a);
+  else
+    gfft::ragged_kernel<float><<<r->grid, r->threads, r->smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? GFFT_OK : GFFT_E_CUDA;
+}
+
+int gfft_ragged_exec(gfft_ragged* r, const void* src, void* dst, gfft_stream stream) {
+  if (!r || r->magic != 0x6A66ED00u) return GFFT_E_INVALID_HANDLE;
+  if (!src || !dst) return GFFT_E_NULL_POINTER;
+  const size_t al = r->dbl ? 16 : 8;
+  if (((uintptr_t)src % al) || ((uintptr_t)dst % al)) return GFFT_E_MISALIGNED;
+  if (src == dst && r->max_passes > 1) {
+    // a single-pass group reads and writes whole transforms, a multi-pass
+    // transform goes through the workspace: both are safe in place except
+    // the first pass of a multi-pass transform writing the workspace while
+    // its input is also the output of the last pass -- also safe, since the
+    // last pass runs after every first-pass tile of that transform.
+  }
+  if (!r->gexec || r->g_src != src || r->g_dst != dst) {
+    if (r->gexec) {
+      cudaGraphExecDestroy(r->gexec);
+      r->gexec = nullptr;
+    }
+    if (r->graph) {
+      cudaGraphDestroy(r->graph);
+      r->graph = nullptr;
+    }
+    if (cudaStreamBeginCapture(r->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GFFT_E_CUDA;
+    int st = ragged_launch(r, src, dst, r->cap_stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(r->cap_stream, &g);
+    if (st != GFFT_OK || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return GFFT_E_CUDA;
+    }
+    r->graph = g;
+    if (cudaGraphInstantiate(&r->gexec, g, 0) != cudaSuccess) return GFFT_E_CUDA;
+    r->g_src = src;
+    r->g_dst = dst;
+  }
+  return cudaGraphLaunch(r->gexec, (cudaStream_t)stream) == cudaSuccess ? GFFT_OK : GFFT_E_CUDA;
+}
+
+int gfft_ragged_get_info(gfft_ragged* r, uint64_t* total_points, uint64_t* items, int* distinct_lengths,
+                         int* max_passes, unsigned* grid) {
+  if (!r || r->magic != 0x6A66ED00u) return GFFT_E_INVALID_HANDLE;
+  if (total_points) *total_points = (uint64_t)r->total;
+  if (items) *items = (uint64_t)r->nitems;
+  if (distinct_lengths) *distinct_lengths = r->nplans;
+  if (max_passes) *max_passes = r->max_passes;
+  if (grid) *grid = r->grid;
+  return GFFT_OK;
+}
+
+int gfft_ragged_get_status(gfft_ragged* r, int* status) {
+  if (!r || r->magic != 0x6A66ED00u) return GFFT_E_INVALID_HANDLE;
+  if (!status) return GFFT_E_NULL_POINTER;
+  if (cudaDeviceSynchronize() != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaMemcpy(status, r->d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return GFFT_E_CUDA;
+  if (cudaMemset(r->d_status, 0, sizeof(int)) != cudaSuccess) return GFFT_E_CUDA;
+  return GFFT_OK;
+}
+
+int gfft_ragged_destroy(gfft_ragged* r) {
+  if (!r || r->magic != 0x6A66ED00u) return GFFT_E_INVALID_HANDLE;
+  r->magic = 0;
+  free_ragged(r);
+  return GFFT_OK;
+}
+
+}  // extern "C"

@@ -25,10 +25,16 @@
 // multiplication", PLDI 1994, round-up method): for d > 1 with
 // l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1 and t = umulhi(x, m),
 // x / d = (t + ((x - t) >> 1)) >> (l - 1) for every 32-bit x.
+#ifdef __CUDACC__
+#define GFFT_HD __host__ __device__
+#else
+#define GFFT_HD
+#endif
+
 struct FastDiv {
   unsigned d, m, l;
 };
-inline FastDiv make_fastdiv(unsigned d) {
+GFFT_HD inline FastDiv make_fastdiv(unsigned d) {
   FastDiv f;
   f.d = d;
   if (d <= 1) {
@@ -90,6 +96,8 @@ struct EngineArgs {
   int debug_no_issue; // test hook: never issue the copies, so the first wait runs out
   FastDiv fd_L;       // L
   FastDiv fd_half;    // L/2 + 1 (real pre/post pass)
+  const long long* lane_off;  // mode 2: element offset of each lane's transform
+  int ldcg;           // read the input through L2 only (data written by other blocks of this launch)
   BlockPass pass[GFFT_MAXP];
 };
 
@@ -116,6 +124,52 @@ struct PlanOpts {
   int max_pass_len = 0;
   int variant = 0;
   int stages = 0;
+  // internal (ragged batches): largest single-pass length and shared-memory budget
+  int max_single = 0;
+  int smem_budget = 0;
+};
+
+// ---- ragged batches: one persistent launch over transforms of many sizes --
+// Per distinct size: the global passes of its plan (in-block radices,
+// twiddle offsets relative to the size's own table block).
+struct RaggedPlan {
+  long long n;
+  int nglobal;
+  int tiles[GFFT_MAXG];    // work items of each global pass (two-pass sizes)
+  int L[GFFT_MAXG], W[GFFT_MAXG], npass[GFFT_MAXG];
+  long long Ns[GFFT_MAXG];
+  long long tab;           // this size's tables, complex elements from the table base
+  long long gtw_lo, gtw_hi, gB;  // relative to tab
+  BlockPass pass[GFFT_MAXG][GFFT_MAXP];
+};
+// One unit of work: global pass `pass` of a plan, over `count` lanes starting
+// at unit `unit0` of transform `transform` (multi-pass sizes), or over
+// `count` whole transforms whose offsets are lane_off[group ..] (single-pass).
+struct RaggedItem {
+  int plan;
+  int pass;
+  int count;
+  int transform;
+  long long unit0;
+  long long group;
+};
+struct RaggedArgs {
+  const void* in;
+  void* out;
+  void* ws;
+  long long ws2_off;          // second workspace (three-pass lengths), elements after ws
+  const void* tab;
+  const RaggedPlan* plans;
+  const RaggedItem* items;
+  const long long* lane_off;  // single-pass groups
+  const long long* offset;    // element offset of every transform
+  int* done;                  // completed tiles per (transform, pass)
+  int* head;                  // queue head
+  int* status;
+  long long nitems;
+  long long spin_limit;
+  int conj;
+  int lanes_max;              // largest W*Lp of any item (shared buffer size)
 };
 
 struct HostPlan {

@@ -157,11 +157,12 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
 
   const int esz = dbl ? 16 : 8;
   const int pad_shift = dbl ? 3 : 4;
-  const long long smem_budget = 160 * 1024;
+  const long long smem_budget = o.smem_budget > 0 ? o.smem_budget : 160 * 1024;
   auto padded = [&](long long L) { return L + (L >> pad_shift) + 1; };
   // largest single-pass length: two padded buffers of one transform
   long long cap1 = dbl ? 4096 : 8192;
   if (o.max_pass_len > 0) cap1 = std::min<long long>(cap1, o.max_pass_len);
+  if (o.max_single > 0) cap1 = std::min<long long>(cap1, o.max_single);
   int lane_w = o.units > 0 ? o.units : (dbl ? 4 : 8);  // 64-byte rows
   if (lane_w > 32) lane_w = 32;
   long long capL = 1;

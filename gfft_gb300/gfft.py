@@ -275,6 +275,56 @@ class TransformObject:
             pass
 
 
+class RaggedBatch:
+    """Transforms of many lengths (back to back, in the order of ``sizes``)
+    in one persistent launch replayed from a CUDA graph (gfft_ragged_*).
+    ``fft(src, dst)`` takes device tensors on the current stream."""
+
+    def __init__(self, sizes, VType=FLOAT, Type=DFT):
+        import numpy as _np
+        self.sizes = _np.ascontiguousarray(_np.asarray(sizes, dtype=_np.uint64))
+        self.VType, self.Type = VType, Type
+        L = _lib.lib()
+        h = ctypes.c_void_p()
+        st = L.gfft_ragged_create(ctypes.byref(h), int(self.sizes.size),
+                                  self.sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), VType.ID, Type.ID)
+        _lib.check(st, "gfft_ragged_create")
+        self._h = h
+        self.total_points = int(self.sizes.sum())
+
+    def info(self):
+        tp, it = ctypes.c_uint64(), ctypes.c_uint64()
+        nd, mp, gr = ctypes.c_int(), ctypes.c_int(), ctypes.c_uint()
+        _lib.check(_lib.lib().gfft_ragged_get_info(self._h, ctypes.byref(tp), ctypes.byref(it), ctypes.byref(nd),
+                                                   ctypes.byref(mp), ctypes.byref(gr)))
+        return {"total_points": tp.value, "items": it.value, "distinct_lengths": nd.value, "max_passes": mp.value,
+                "grid": gr.value}
+
+    def status(self):
+        st = ctypes.c_int(-1)
+        _lib.check(_lib.lib().gfft_ragged_get_status(self._h, ctypes.byref(st)))
+        return st.value
+
+    def fft(self, src, dst):
+        import torch
+        stream = torch.cuda.current_stream(src.device).cuda_stream
+        _lib.check(_lib.lib().gfft_ragged_exec(self._h, ctypes.c_void_p(src.data_ptr()),
+                                               ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(stream)),
+                   "gfft_ragged_exec")
+        return dst
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().gfft_ragged_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Transform:
     """``Transform<N, VType, Type, Dim, Parall, Place>`` (src/gfftgen.h:46-87):
     ``Transform(...).Instance()`` / ``Create()`` return a new object."""

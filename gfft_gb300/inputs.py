@@ -71,3 +71,34 @@ def tone_mix(seed: int, n: int, batch: int, amp: float = 1e-4, tones: int = 8) -
     inter[1::2] = sig.imag
     out.reshape(batch, 2 * n)[:] = inter
     return out
+
+
+def smooth235(limit: int) -> np.ndarray:
+    """All 2^a 3^b 5^c <= limit, ascending."""
+    out = []
+    p2 = 1
+    while p2 <= limit:
+        p3 = p2
+        while p3 <= limit:
+            p5 = p3
+            while p5 <= limit:
+                out.append(p5)
+                p5 *= 5
+            p3 *= 3
+        p2 *= 2
+    return np.array(sorted(out), dtype=np.int64)
+
+
+def ragged_sizes(seed: int, count: int, lo: int = 6, hi: int = 18) -> np.ndarray:
+    """``count`` lengths log-uniform in [2^lo, 2^hi], each snapped to the
+    nearest 5-smooth value inside that range (ties go down)."""
+    z = _mix(seed, 0, count)
+    u = (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    target = 2.0 ** (lo + u * (hi - lo))
+    cand = smooth235(2 ** hi)
+    cand = cand[cand >= 2 ** lo]
+    idx = np.searchsorted(cand, target)
+    idx = np.clip(idx, 1, len(cand) - 1)
+    below, above = cand[idx - 1], cand[idx]
+    pick = np.where(target - below <= above - target, below, above)
+    return pick.astype(np.int64)

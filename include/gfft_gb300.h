@@ -139,6 +139,27 @@ int gfft_get_device_status(gfft_handle handle, int* status);
  * GFFT_E_TIMEOUT) in *status.  No reference counterpart. */
 int gfft_selftest_bounded_wait(long long spin_limit, int* status);
 
+/* ---- ragged batches -------------------------------------------------------
+ * Transforms of many different lengths in ONE persistent launch driven by a
+ * device work queue over (length, pass, tile), replayed from a CUDA graph.
+ * Replaces running one reference object per length in turn (objects from
+ * GenerateTransform over an NList, src/gfftgen.h:189-231, each fft() call
+ * parallelised only inside one transform by the OpenMP policy,
+ * src/gfftomp.h:41-189).  Data: the `count` transforms lie back to back in
+ * the order of `sizes` (interleaved complex).  DFT (0) or IDFT (1). */
+typedef struct gfft_ragged gfft_ragged;
+
+int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* sizes, int vtype_id, int trans_id);
+/* Device pointers; the launch sequence is captured into a CUDA graph on the
+ * first call for a (src, dst) pair and replayed afterwards. */
+int gfft_ragged_exec(gfft_ragged* handle, const void* src, void* dst, gfft_stream stream);
+int gfft_ragged_get_info(gfft_ragged* handle, uint64_t* total_points, uint64_t* items, int* distinct_lengths,
+                         int* max_passes, unsigned* grid);
+/* Device status word of the persistent kernel (GFFT_E_TIMEOUT if a bounded
+ * wait between passes ran out); synchronises, reads and clears it. */
+int gfft_ragged_get_status(gfft_ragged* handle, int* status);
+int gfft_ragged_destroy(gfft_ragged* handle);
+
 /* A transform that allocates nothing.  No counterpart in the reference (its
  * transform objects never touch device memory).
  *

@@ -1,0 +1,98 @@
+"""GPU: ragged batches (many lengths, one persistent launch from a CUDA
+graph) against numpy's FP64 FFT per transform and against the per-length
+transform objects."""
+import numpy as np
+import pytest
+
+from gfft_gb300 import inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def tol(n, dbl):
+    return (2e-15 if dbl else 6e-7) * max(1.0, np.log2(max(n, 2)))
+
+
+def _check(y, x, sizes, sign, dbl, scale=1.0):
+    off = 0
+    worst = 0.0
+    for n in sizes:
+        n = int(n)
+        xs = x[2 * off:2 * (off + n)].astype(np.float64)
+        c = xs[0::2] + 1j * xs[1::2]
+        f = np.fft.fft(c) if sign > 0 else np.fft.ifft(c)
+        ref = np.empty(2 * n)
+        ref[0::2], ref[1::2] = f.real, f.imag
+        got = y[2 * off:2 * (off + n)].astype(np.float64)
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300)
+        assert err <= tol(n, dbl), (n, err)
+        worst = max(worst, err)
+        off += n
+    return worst
+
+
+@pytest.mark.parametrize("dbl", [0, 1])
+def test_ragged_matches_exact(cuda, dbl):
+    import torch
+    from gfft_gb300 import gfft as G
+    sizes = np.concatenate([inputs.ragged_sizes(71, 240, 6, 13), inputs.ragged_sizes(72, 12, 13, 18),
+                            [1, 2, 3, 64, 4096, 4097 - 1, 2 ** 18]])
+    vt = G.DOUBLE if dbl else G.FLOAT
+    dt = torch.float64 if dbl else torch.float32
+    total = int(sizes.sum())
+    x = inputs.uniform(5, 2 * total)
+    xt = torch.from_numpy(x).to(dt).cuda()
+    fwd = G.RaggedBatch(sizes, vt, G.DFT)
+    inv = G.RaggedBatch(sizes, vt, G.IDFT)
+    info = fwd.info()
+    assert info["total_points"] == total and info["max_passes"] >= 2
+    y = torch.empty_like(xt)
+    fwd.fft(xt, y)
+    torch.cuda.synchronize()
+    _check(y.cpu().numpy(), xt.cpu().numpy(), sizes, 1, dbl)
+    z = torch.empty_like(xt)
+    inv.fft(y, z)
+    torch.cuda.synchronize()
+    _check(z.cpu().numpy(), y.cpu().numpy(), sizes, -1, dbl)
+    assert fwd.status() == 0 and inv.status() == 0
+
+
+def test_ragged_graph_replay_and_new_pointers(cuda):
+    import torch
+    from gfft_gb300 import gfft as G
+    sizes = inputs.ragged_sizes(81, 64, 6, 16)
+    total = int(sizes.sum())
+    rb = G.RaggedBatch(sizes, G.FLOAT, G.DFT)
+    a = torch.from_numpy(inputs.uniform(1, 2 * total)).float().cuda()
+    out = torch.empty_like(a)
+    rb.fft(a, out)                      # captures the graph
+    b = torch.from_numpy(inputs.uniform(2, 2 * total)).float().cuda()
+    a.copy_(b)
+    rb.fft(a, out)                      # replays it on new data
+    torch.cuda.synchronize()
+    _check(out.cpu().numpy(), b.cpu().numpy(), sizes, 1, 0)
+    out2 = torch.empty_like(a)
+    rb.fft(b, out2)                     # new pointers: captured again
+    torch.cuda.synchronize()
+    assert torch.equal(out, out2)
+    assert rb.status() == 0
+
+
+def test_ragged_equals_per_length_objects(cuda):
+    import torch
+    from gfft_gb300 import gfft as G
+    sizes = np.array([4096, 1000, 8192, 786432 // 3, 60, 4096])
+    total = int(sizes.sum())
+    x = torch.from_numpy(inputs.uniform(3, 2 * total)).float().cuda()
+    y = torch.empty_like(x)
+    G.RaggedBatch(sizes, G.FLOAT, G.DFT).fft(x, y)
+    off = 0
+    for n in sizes:
+        n = int(n)
+        seg = slice(2 * off, 2 * (off + n))
+        want = torch.empty(2 * n, device="cuda")
+        G.TransformObject(n, G.FLOAT, G.DFT).fft(x[seg].contiguous(), want)
+        torch.cuda.synchronize()
+        r = (torch.linalg.vector_norm(y[seg] - want) / torch.linalg.vector_norm(want)).item()
+        assert r <= tol(n, 0), (n, r)
+        off += n
