@@ -253,6 +253,20 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.smem = (size_t)(S * tb_al + ((W * padded(gp.L) * esz + 7) & ~7LL) + 8 * S);
       }
     }
+    // pipelined column tiles for the passes of a multi-pass length
+    if (gp.mode == 1 && (o.variant == 0 || o.variant == 4) && o.units == 0 && o.threads == 0) {
+      const long long TILE = dbl ? 2048 : 4096;
+      const long long stride = n / gp.L;
+      long long W = 1;
+      while (W * 2 * gp.L <= TILE && W * 2 <= stride && W * 2 <= 8) W *= 2;
+      if (W * gp.L <= TILE) {
+        gp.variant = 4;
+        gp.units = (int)W;
+        gp.threads = 256;
+        gp.ntiles = (batch * stride + W - 1) / W;
+        gp.smem = (size_t)(3 * W * padded(gp.L) * esz);  // prefetch buffer + ping-pong pair
+      }
+    }
     // length-specialised variant: default radix order, L in the compiled set
     const long long TILE = dbl ? 2048 : 4096;
     bool spec = gp.variant == 2 && (o.variant == 0 || o.variant == 3) && o.units == 0 && o.threads == 0 &&

@@ -440,3 +440,21 @@ def test_cpp_facade_on_gpu(cuda):
     r = subprocess.run([exe, "gpu"], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "facade ok (gpu)" in r.stdout
+
+
+@pytest.mark.parametrize("n,dbl,B", [(786432, 0, 3), (390625, 1, 2), (248832, 0, 5), (1 << 20, 1, 1),
+                                     (12288, 0, 7), (1 << 24, 0, 1), (3 * 5 * 7 * 11 * 13 * 16, 0, 1)])
+def test_multipass_pipelined_matches_engine(cuda, oracle, n, dbl, B):
+    """The prefetching column-tile kernel (variant 4) against the one-tile-per-
+    block engine (variant 1), forward and inverse, with a ragged last tile."""
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    x = inputs.gaussian(91 + n, 2 * n * B).astype(dt)
+    for tr in (0, 1):
+        fast = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+        gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
+        assert rel(fast, gen) <= tol(n, dbl), (n, tr, rel(fast, gen))
+    if n <= 1 << 20:
+        ex = oracle.fft_ld(x[:2 * n].astype(np.float64), n, 1, 1)
+        y = run_gpu(cuda, n, vt, 0, 1, x[:2 * n])
+        assert rel(y, ex) <= tol(n, dbl)
