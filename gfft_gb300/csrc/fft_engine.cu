@@ -110,6 +110,7 @@ extern "C" int gfft_engine_setup(int dbl, size_t max_smem) {
 
 extern "C" int gfft_engine_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                   cudaStream_t stream) {
+  cudaGetLastError();  // clear a stale error of an earlier, unrelated call
   if (dbl) gfft::engine_kernel<double><<<grid, threads, smem, stream>>>(*a);
   else gfft::engine_kernel<float><<<grid, threads, smem, stream>>>(*a);
   return (int)cudaGetLastError();
@@ -117,6 +118,7 @@ extern "C" int gfft_engine_launch(int dbl, const EngineArgs* a, unsigned grid, u
 
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream) {
+  cudaGetLastError();  // clear a stale error of an earlier, unrelated call
   long long total = (n / 2 + 1) * batch;
   unsigned threads = 256;
   long long blocks = (total + threads - 1) / threads;

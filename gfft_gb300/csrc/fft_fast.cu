@@ -289,6 +289,7 @@ extern "C" int gfft_fast_occupancy(int dbl, int threads, size_t smem) {
 
 extern "C" int gfft_fast_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                 cudaStream_t stream) {
+  cudaGetLastError();  // clear a stale error of an earlier, unrelated call
   if (dbl) gfft::fast_kernel<double><<<grid, threads, smem, stream>>>(*a);
   else gfft::fast_kernel<float><<<grid, threads, smem, stream>>>(*a);
   return (int)cudaGetLastError();

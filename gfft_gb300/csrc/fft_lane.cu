@@ -154,6 +154,7 @@ extern "C" int gfft_lane_occupancy(int dbl, int threads, size_t smem) {
 
 extern "C" int gfft_lane_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                 cudaStream_t stream) {
+  cudaGetLastError();  // clear a stale error of an earlier, unrelated call
   if (dbl) gfft::lane_kernel<double><<<grid, threads, smem, stream>>>(*a);
   else gfft::lane_kernel<float><<<grid, threads, smem, stream>>>(*a);
   return (int)cudaGetLastError();

@@ -313,6 +313,7 @@ extern "C" int gfft_exec_noalloc(uint64_t n, int vtype_id, int trans_id, uint64_
   }
   cudaStream_t s = (cudaStream_t)stream;
   if (sl.n > 0) {
+    cudaGetLastError();  // clear a stale error of an earlier, unrelated call
     fill_tables<<<64, 256, 0, s>>>(sl);
     if (cudaGetLastError() != cudaSuccess) return GFFT_E_CUDA;
   }

@@ -370,11 +370,16 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (r->smem + 4096 > (size_t)maxopt) {  // dynamic buffers plus the kernel's static shared memory
+    free_ragged(r);
+    return GFFT_E_INVALID_SIZE;
+  }
   cudaError_t ce = r->dbl ? cudaFuncSetAttribute(gfft::ragged_kernel<double>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt)
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r->smem)
                           : cudaFuncSetAttribute(gfft::ragged_kernel<float>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r->smem);
   if (ce != cudaSuccess) {
+    cudaGetLastError();  // do not leave the failure for the next launch to report
     free_ragged(r);
     return GFFT_E_CUDA;
   }
@@ -412,6 +417,7 @@ static int ragged_launch(gfft_ragged* r, const void* src, void* dst, cudaStream_
   a.spin_limit = 1LL << 24;
   a.conj = r->inverse;
   a.lanes_max = r->lanes_max;
+  cudaGetLastError();  // clear a stale error of an earlier, unrelated call
   if (r->dbl)
     gfft::ragged_kernel<double><<<r->grid, r->threads, r->smem, s>>>(a);
   else
