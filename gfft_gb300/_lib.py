@@ -24,7 +24,10 @@ STATUS_NAMES = {
 EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
             "gfft_get_info", "gfft_plan_query", "gfft_get_device_status", "gfft_selftest_bounded_wait",
             "gfft_exec_noalloc", "gfft_ragged_create", "gfft_ragged_exec", "gfft_ragged_get_info",
-            "gfft_ragged_get_status", "gfft_ragged_destroy", "gfft_version"]
+            "gfft_ragged_get_status", "gfft_ragged_destroy", "gfft_tune_candidates", "gfft_tune_measure",
+            "gfft_plan_features", "gfft_mlp_create", "gfft_mlp_num_params", "gfft_mlp_get_params", "gfft_mlp_set_params",
+            "gfft_mlp_train", "gfft_mlp_predict", "gfft_mlp_gradients", "gfft_mlp_destroy", "gfft_version"]
+NFEAT = 24
 
 
 class PlanOpts(ctypes.Structure):
@@ -88,6 +91,18 @@ def lib():
                                            ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_uint)]
         L.gfft_ragged_get_status.argtypes = [vp, ctypes.POINTER(ci)]
         L.gfft_ragged_destroy.argtypes = [vp]
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.gfft_tune_candidates.argtypes = [u64, ci, ci, ci, u64, ctypes.POINTER(PlanOpts), ci, ctypes.POINTER(ci)]
+        L.gfft_tune_measure.argtypes = [u64, ci, ci, ci, u64, ctypes.POINTER(PlanOpts), ci, vp, vp, ci, fp]
+        L.gfft_plan_features.argtypes = [u64, ci, ci, ci, u64, ctypes.POINTER(PlanOpts), fp]
+        L.gfft_mlp_create.argtypes = [ctypes.POINTER(vp), ci, ci, ci, u64]
+        L.gfft_mlp_num_params.argtypes = [vp]
+        L.gfft_mlp_get_params.argtypes = [vp, fp]
+        L.gfft_mlp_set_params.argtypes = [vp, fp]
+        L.gfft_mlp_train.argtypes = [vp, fp, fp, ci, ci, ctypes.c_float, fp]
+        L.gfft_mlp_predict.argtypes = [vp, fp, ci, fp]
+        L.gfft_mlp_gradients.argtypes = [vp, fp, fp, ci, fp, fp]
+        L.gfft_mlp_destroy.argtypes = [vp]
         for name in EXPORTED:
             getattr(L, name).restype = getattr(L, name).restype or ci
         L.gfft_strerror.restype = ctypes.c_char_p

@@ -1,0 +1,211 @@
+"""Autotuner and learned planner over the C ABI.
+
+- ``candidates``: the distinct plans reachable through the plan options;
+- ``measure``: exhaustive measured search (every candidate timed with CUDA
+  events in the library);
+- ``CostModel``: a 3 x 64 FP32 MLP on ``gfft_plan_features``, trained and
+  evaluated on the GPU by the library's own kernels (``gfft_mlp_*``), with the
+  feature normalisation kept beside the weights; ``save`` / ``load`` persist
+  both (the tuner's only state, with the timing table);
+- ``choose``: the plan the model ranks first, or the best measured among its
+  top ``k`` (a pruned search; ``k=None`` falls back to the exhaustive one).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+
+import numpy as np
+
+from . import _lib
+
+OPT_FIELDS = ["radix_order", "max_radix", "threads_per_block", "units_per_block", "max_pass_len", "kernel_variant",
+              "stages", "blocks_per_sm"]
+
+
+def _opts_to_dict(o: _lib.PlanOpts) -> dict:
+    return {k: int(getattr(o, k)) for k in OPT_FIELDS if int(getattr(o, k))}
+
+
+def candidates(n, vtype=1, trans=0, place=1, batch=1, max_cands=64):
+    arr = (_lib.PlanOpts * max_cands)()
+    cnt = ctypes.c_int()
+    _lib.check(_lib.lib().gfft_tune_candidates(n, vtype, trans, place, batch, arr, max_cands, ctypes.byref(cnt)),
+               "gfft_tune_candidates")
+    return [_opts_to_dict(arr[i]) for i in range(cnt.value)]
+
+
+def features(n, vtype, trans, place, batch, opts: dict) -> np.ndarray:
+    f = np.zeros(_lib.NFEAT, dtype=np.float32)
+    o = _lib.make_opts(opts) if opts else None
+    _lib.check(_lib.lib().gfft_plan_features(n, vtype, trans, place, batch, ctypes.byref(o) if o else None,
+                                             f.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "gfft_plan_features")
+    return f
+
+
+def measure(n, vtype, trans, place, batch, cands, reps=5, src=None, dst=None):
+    """Time every candidate (ms per launch) on device buffers (allocated here
+    with torch when not given)."""
+    import torch
+    if src is None:
+        dt = torch.float64 if vtype in (0, 2) else torch.float32
+        src = torch.rand(2 * n * batch, device="cuda", dtype=dt)
+        dst = torch.empty_like(src)
+    arr = (_lib.PlanOpts * len(cands))()
+    for i, c in enumerate(cands):
+        for k, v in c.items():
+            setattr(arr[i], k, int(v))
+    ms = np.zeros(len(cands), dtype=np.float32)
+    _lib.check(_lib.lib().gfft_tune_measure(n, vtype, trans, place, batch, arr, len(cands),
+                                            ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(dst.data_ptr()), reps,
+                                            ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "gfft_tune_measure")
+    return ms
+
+
+class MLP:
+    """The library's GPU-trained perceptron (gfft_mlp_*)."""
+
+    def __init__(self, nin=_lib.NFEAT, width=64, depth=3, seed=1):
+        self.nin, self.width, self.depth = nin, width, depth
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().gfft_mlp_create(ctypes.byref(h), nin, width, depth, seed), "gfft_mlp_create")
+        self._h = h
+        self.nparams = _lib.lib().gfft_mlp_num_params(h)
+
+    @staticmethod
+    def _fp(a):
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def params(self):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        _lib.check(_lib.lib().gfft_mlp_get_params(self._h, self._fp(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _lib.check(_lib.lib().gfft_mlp_set_params(self._h, self._fp(p)))
+
+    def train(self, X, y, epochs=2000, lr=3e-3):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = ctypes.c_float()
+        _lib.check(_lib.lib().gfft_mlp_train(self._h, self._fp(X), self._fp(y), len(y), epochs, lr,
+                                             ctypes.byref(loss)), "gfft_mlp_train")
+        return loss.value
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros(len(X), dtype=np.float32)
+        _lib.check(_lib.lib().gfft_mlp_predict(self._h, self._fp(X), len(X), self._fp(out)), "gfft_mlp_predict")
+        return out
+
+    def gradients(self, X, y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        loss = ctypes.c_float()
+        _lib.check(_lib.lib().gfft_mlp_gradients(self._h, self._fp(X), self._fp(y), len(y), self._fp(g),
+                                                 ctypes.byref(loss)), "gfft_mlp_gradients")
+        return g, loss.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().gfft_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CostModel:
+    """log(ms) of a plan from its features; inputs standardised with the
+    training set's mean and spread."""
+
+    def __init__(self, seed=1):
+        self.net = MLP(seed=seed)
+        self.mu = np.zeros(_lib.NFEAT, dtype=np.float32)
+        self.sd = np.ones(_lib.NFEAT, dtype=np.float32)
+
+    def fit(self, X, ms, epochs=3000, lr=3e-3):
+        X = np.asarray(X, dtype=np.float32)
+        self.mu = X.mean(0)
+        self.sd = np.where(X.std(0) > 1e-6, X.std(0), 1.0).astype(np.float32)
+        return self.net.train((X - self.mu) / self.sd, np.log(np.asarray(ms, dtype=np.float32)), epochs, lr)
+
+    def predict_ms(self, X):
+        X = (np.asarray(X, dtype=np.float32) - self.mu) / self.sd
+        return np.exp(self.net.predict(X))
+
+    def save(self, path):
+        np.savez(path, params=self.net.params(), mu=self.mu, sd=self.sd)
+
+    @classmethod
+    def load(cls, path):
+        d = np.load(path)
+        m = cls()
+        m.net.set_params(d["params"])
+        m.mu, m.sd = d["mu"], d["sd"]
+        return m
+
+
+def choose(model, n, vtype=1, trans=0, place=1, batch=1, k=1, reps=5):
+    """Plan options for (n, ...): the model's first choice (k=1), the best
+    measured of its top k, or the exhaustive measured best (model=None)."""
+    cands = candidates(n, vtype, trans, place, batch)
+    if model is None:
+        ms = measure(n, vtype, trans, place, batch, cands, reps)
+        ok = np.where(ms > 0, ms, np.inf)
+        return cands[int(np.argmin(ok))], float(np.min(ok))
+    X = np.stack([features(n, vtype, trans, place, batch, c) for c in cands])
+    pred = model.predict_ms(X)
+    order = np.argsort(pred)[:max(1, k)]
+    if len(order) == 1:
+        return cands[int(order[0])], float(pred[order[0]])
+    sub = [cands[int(i)] for i in order]
+    ms = measure(n, vtype, trans, place, batch, sub, reps)
+    ok = np.where(ms > 0, ms, np.inf)
+    return sub[int(np.argmin(ok))], float(np.min(ok))
+
+
+def timing_table(sizes, vtype=1, batch_points=1 << 20, reps=5, log=None):
+    """Measured timings of every candidate of every size: rows of
+    (n, batch, opts, features, ms).  batch = max(1, batch_points // n)."""
+    rows = []
+    for n in sizes:
+        n = int(n)
+        batch = max(1, batch_points // n)
+        cands = candidates(n, vtype, 0, 1, batch)
+        ms = measure(n, vtype, 0, 1, batch, cands, reps)
+        for c, t in zip(cands, ms):
+            if t > 0:
+                rows.append({"n": n, "batch": batch, "opts": c, "ms": float(t),
+                             "features": features(n, vtype, 0, 1, batch, c).tolist()})
+        if log:
+            log(n, len(cands))
+    return rows
+
+
+def save_table(rows, path):
+    with open(path, "w") as f:
+        json.dump(rows, f)
+
+
+def load_table(path):
+    with open(path) as f:
+        return json.load(f)
+
+
+def default_plan_ms(row_group):
+    """Time of the planner's default plan (no options) within a size's rows."""
+    for r in row_group:
+        if not r["opts"]:
+            return r["ms"]
+    return None
+
+
+def gflops(n, batch, ms):
+    return 5.0 * n * math.log2(max(n, 2)) * batch / ms / 1e6

@@ -139,6 +139,41 @@ int gfft_get_device_status(gfft_handle handle, int* status);
  * GFFT_E_TIMEOUT) in *status.  No reference counterpart. */
 int gfft_selftest_bounded_wait(long long spin_limit, int* status);
 
+/* ---- autotuner and learned cost model -------------------------------------
+ * No reference counterpart (the reference's plan is its compile-time factor
+ * list, src/gfftfactor.h:160-169).  Candidates are the distinct plans reached
+ * through gfft_plan_opts; gfft_tune_measure times each on caller-provided
+ * device buffers (exhaustive measured search, `reps` launches each after one
+ * warm-up); failed candidates get -1. */
+#define GFFT_NFEAT 24
+int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
+                         gfft_plan_opts* cands, int max_cands, int* ncands);
+int gfft_tune_measure(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
+                      const gfft_plan_opts* cands, int ncands, const void* d_src, void* d_dst, int reps,
+                      float* ms_out);
+/* Feature vector (GFFT_NFEAT floats) of the plan these options give:
+ * log2 N, exponents of 2/3/5/7, log2 batch, log2 lane stride of the first
+ * pass, dtype, global passes, counts of radices 16/8/4/2/3/5/7 and of generic
+ * primes, log2 threads per transform, kernel variant, stages, log2 units,
+ * radix order, log2 bytes, log2 pass-length cap.  No GPU needed. */
+int gfft_plan_features(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
+                       const gfft_plan_opts* opts, float* features);
+
+/* A multi-layer perceptron cost model (FP32, `depth` hidden ReLU layers of
+ * `width`, one linear output) trained on the GPU by the library's own
+ * forward / backward / Adam kernels. */
+typedef struct gfft_mlp gfft_mlp;
+int gfft_mlp_create(gfft_mlp** m, int nin, int width, int depth, uint64_t seed);
+int gfft_mlp_num_params(gfft_mlp* m);
+int gfft_mlp_get_params(gfft_mlp* m, float* params);
+int gfft_mlp_set_params(gfft_mlp* m, const float* params);
+/* full-batch Adam on the mean squared error; X is n x nin row-major (host) */
+int gfft_mlp_train(gfft_mlp* m, const float* X, const float* y, int n, int epochs, float lr, float* final_loss);
+int gfft_mlp_predict(gfft_mlp* m, const float* X, int n, float* y_out);
+/* gradient of the mean squared error w.r.t. every parameter (for checks) */
+int gfft_mlp_gradients(gfft_mlp* m, const float* X, const float* y, int n, float* grad_out, float* loss_out);
+int gfft_mlp_destroy(gfft_mlp* m);
+
 /* ---- ragged batches -------------------------------------------------------
  * Transforms of many different lengths in ONE persistent launch driven by a
  * device work queue over (length, pass, tile), replayed from a CUDA graph.

@@ -1,0 +1,67 @@
+"""GPU: the cost model's kernels against the FP64 reference, its training,
+and the learned planner against exhaustive measured search."""
+import numpy as np
+import pytest
+
+from gfft_gb300 import tuner
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_forward_and_gradients_match_reference(cuda):
+    from oracle import mlp_ref
+    m = tuner.MLP(nin=24, width=64, depth=3, seed=7)
+    p = m.params()
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(500, 24)).astype(np.float32)
+    y = rng.normal(size=500).astype(np.float32)
+    pred = m.predict(X)
+    ref = mlp_ref.forward(p, X, 24, 64, 3)
+    assert np.max(np.abs(pred - ref)) <= 1e-4 * max(1.0, np.max(np.abs(ref)))
+    g, loss = m.gradients(X, y)
+    gr = mlp_ref.gradients(p, X, y, 24, 64, 3)
+    rel = np.linalg.norm(g - gr) / np.linalg.norm(gr)
+    assert rel <= 1e-4, rel
+    assert abs(loss - np.mean((ref - y) ** 2)) <= 1e-4 * max(1.0, loss)
+
+
+def test_mlp_training_fits_smooth_target(cuda):
+    rng = np.random.default_rng(2)
+    X = rng.uniform(-1, 1, size=(1500, 24)).astype(np.float32)
+    y = (np.sin(2 * X[:, 0]) + 0.5 * X[:, 1] * X[:, 2]).astype(np.float32)
+    m = tuner.MLP(seed=3)
+    l0 = float(np.mean((m.predict(X) - y) ** 2))
+    l1 = m.train(X, y, epochs=1500, lr=3e-3)
+    assert l1 < 0.1 * l0 and l1 < 0.02, (l0, l1)
+
+
+def test_learned_planner_regret(cuda):
+    """Train on measured plans of some sizes, choose plans for held-out sizes,
+    compare with exhaustive search and with the planner's default plan."""
+    rng = np.random.default_rng(5)
+    pool = [n for n in (2 ** a * 3 ** b * 5 ** c for a in range(4, 19) for b in range(0, 4) for c in range(0, 3))
+            if 256 <= n <= 1 << 20]
+    pool = sorted(set(pool))
+    sizes = rng.choice(pool, 60, replace=False)
+    train_sizes, test_sizes = sizes[:44], sizes[44:]
+    rows = tuner.timing_table(train_sizes, batch_points=1 << 20, reps=3)
+    X = np.array([r["features"] for r in rows], dtype=np.float32)
+    ms = np.array([r["ms"] for r in rows], dtype=np.float32)
+    model = tuner.CostModel(seed=11)
+    loss = model.fit(X, ms, epochs=2500)
+    assert loss < 0.5
+    regrets, base = [], []
+    for n in test_sizes:
+        n = int(n)
+        b = max(1, (1 << 20) // n)
+        cands = tuner.candidates(n, 1, 0, 1, b)
+        t = tuner.measure(n, 1, 0, 1, b, cands, reps=5)
+        best = float(np.min(t[t > 0]))
+        Xc = np.stack([tuner.features(n, 1, 0, 1, b, c) for c in cands])
+        pick = int(np.argmin(model.predict_ms(Xc)))
+        regrets.append(t[pick] / best - 1)
+        base.append(t[cands.index({})] / best - 1)
+    mean_model, mean_default = float(np.mean(regrets)), float(np.mean(base))
+    print("learned planner regret %.3f, default plan regret %.3f" % (mean_model, mean_default))
+    assert mean_model <= 0.25
+    assert mean_model <= mean_default + 0.05

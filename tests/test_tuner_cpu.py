@@ -1,0 +1,52 @@
+"""CPU: tuner candidate enumeration and plan features (no GPU), and the FP64
+reference of the cost model pinned by finite differences."""
+import numpy as np
+
+from gfft_gb300 import _lib
+from gfft_gb300 import tuner
+
+
+def test_candidates_distinct_and_plannable():
+    for n in (4096, 786432, 1000, 1 << 20):
+        c = tuner.candidates(n, 1, 0, 1, 4)
+        assert 3 <= len(c) <= 64
+        assert {} in c  # the planner's default is always a candidate
+        shapes = set()
+        for o in c:
+            d = _lib.plan_query(n, 1, 0, 1, 4, o or None)
+            key = (tuple(d["pass_len"]), tuple(map(tuple, d["radices"])), tuple(d["kernel_variant"]),
+                   tuple(d["units"]), o.get("stages", 0))
+            assert key not in shapes
+            shapes.add(key)
+
+
+def test_features():
+    f = tuner.features(2 ** 10 * 3 ** 5, 1, 0, 1, 8, {})
+    assert f.shape == (_lib.NFEAT,)
+    assert abs(f[0] - np.log2(2 ** 10 * 3 ** 5)) < 1e-5
+    assert list(f[1:5]) == [10, 5, 0, 0]
+    assert f[5] == 3 and f[7] == 0 and f[8] == 2
+    assert f[9:16].sum() >= 4  # radices counted
+    g = tuner.features(4096, 0, 0, 1, 1, {"max_radix": 4})
+    assert g[7] == 1 and g[11] == 6  # six radix-4 passes, FP64
+
+
+def test_mlp_reference_gradients_finite_difference():
+    from oracle import mlp_ref
+    rng = np.random.default_rng(0)
+    nin, width, depth = 5, 7, 3
+    npar = sum((nin if l == 0 else width) * (1 if l == depth else width) + (1 if l == depth else width)
+               for l in range(depth + 1))
+    p = rng.normal(size=npar) * 0.5
+    X = rng.normal(size=(13, nin))
+    y = rng.normal(size=13)
+    g = mlp_ref.gradients(p, X, y, nin, width, depth)
+
+    def loss(q):
+        return np.mean((mlp_ref.forward(q, X, nin, width, depth) - y) ** 2)
+
+    for i in rng.choice(npar, 40, replace=False):
+        e = np.zeros(npar)
+        e[i] = 1e-6
+        fd = (loss(p + e) - loss(p - e)) / 2e-6
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])
