@@ -53,6 +53,11 @@ def parse():
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    p.add_argument("--planner", action="store_true",
+                   help="learned-planner evaluation: train the cost model on timed plans, regret on held-out sizes")
+    p.add_argument("--planner-train", type=int, default=150, help="training sizes (about 13 plans each)")
+    p.add_argument("--planner-test", type=int, default=200, help="held-out sizes up to 2^27")
+    p.add_argument("--planner-out", default="", help="directory for the timing table and model weights")
     p.add_argument("--only", default="", help="with --suite: run the configurations whose name contains this")
     p.add_argument("--suite", action="store_true",
                    help="time every configuration of the workload list (one JSON line each) instead of the headline")
@@ -349,8 +354,104 @@ def suite_cpu(n, batch, dbl, tr, pl, xh):
     return {"GFLOP/s": fl / dt / 1e9, "cores": pyoracle.num_threads(), "kind": "port", "sample_batch": sample}
 
 
+def _smooth_pool(limit, lo=256):
+    out = set()
+    p2 = 1
+    while p2 <= limit:
+        p3 = p2
+        while p3 <= limit:
+            p5 = p3
+            while p5 <= limit:
+                p7 = p5
+                while p7 <= limit:
+                    if p7 >= lo:
+                        out.add(p7)
+                    p7 *= 7
+                p5 *= 5
+            p3 *= 3
+        p2 *= 2
+    return sorted(out)
+
+
+def run_planner(args):
+    """C5: the cost model trained on autotuner-timed plans (FP32), then plans
+    chosen for held-out sizes up to one 2^27 transform; regret against the
+    exhaustive measured search, the default plan's regret beside it."""
+    import numpy as np
+
+    import gfft_gb300
+    from gfft_gb300 import tuner
+    gfft_gb300.build()
+    rng = np.random.default_rng(0x5EED0005)
+    train_pool = _smooth_pool(1 << 22)
+    test_pool = [n for n in _smooth_pool(1 << 27, 1024)]
+    # log-uniform choice over each pool
+    def pick(pool, k):
+        logs = np.log2(np.array(pool, dtype=np.float64))
+        target = rng.uniform(logs.min(), logs.max(), size=4 * k)
+        idx = np.unique(np.searchsorted(logs, target).clip(0, len(pool) - 1))
+        rng.shuffle(idx)
+        return [pool[i] for i in idx[:k]]
+    train_sizes = pick(train_pool, args.planner_train)
+    test_sizes = [n for n in pick(test_pool, args.planner_test) if n not in set(train_sizes)]
+    if (1 << 27) not in test_sizes:
+        test_sizes[-1:] = [1 << 27]
+    t0 = time.perf_counter()
+    rows = tuner.timing_table(train_sizes, vtype=1, batch_points=1 << 21, reps=3)
+    t_collect = time.perf_counter() - t0
+    X = np.array([r["features"] for r in rows], dtype=np.float32)
+    ms = np.array([r["ms"] for r in rows], dtype=np.float32)
+    model = tuner.CostModel(seed=7)
+    t0 = time.perf_counter()
+    loss = model.fit(X, ms, epochs=4000, lr=3e-3)
+    t_train = time.perf_counter() - t0
+    res = []
+    for n in test_sizes:
+        b = max(1, (1 << 20) // n)
+        cands = tuner.candidates(n, 1, 0, 1, b)
+        t = tuner.measure(n, 1, 0, 1, b, cands, reps=3)
+        ok = t > 0
+        best = float(np.min(t[ok]))
+        Xc = np.stack([tuner.features(n, 1, 0, 1, b, c) for c in cands])
+        pred = model.predict_ms(Xc)
+        pred = np.where(ok, pred, np.inf)
+        order = np.argsort(pred)
+        top1 = float(t[order[0]])
+        top3 = float(np.min(t[order[:3]][t[order[:3]] > 0]))
+        dflt = float(t[cands.index({})])
+        res.append({"n": n, "batch": b, "candidates": len(cands), "best_ms": best, "model_ms": top1,
+                    "pruned3_ms": top3, "default_ms": dflt, "best_gflops": tuner.gflops(n, b, best),
+                    "model_gflops": tuner.gflops(n, b, top1)})
+    reg = np.array([r["model_ms"] / r["best_ms"] - 1 for r in res])
+    reg3 = np.array([r["pruned3_ms"] / r["best_ms"] - 1 for r in res])
+    regd = np.array([r["default_ms"] / r["best_ms"] - 1 for r in res])
+    big = [r for r in res if r["n"] == 1 << 27]
+    line = {"config": "c5 learned planner, FP32, %d training sizes (%d timed plans), %d held-out sizes <= 2^27"
+                      % (len(train_sizes), len(rows), len(res)),
+            "train_rows": len(rows), "collect_s": t_collect, "train_s": t_train, "train_mse_log_ms": loss,
+            "regret_model_mean": float(reg.mean()), "regret_model_median": float(np.median(reg)),
+            "regret_model_p90": float(np.quantile(reg, 0.9)), "within_5pct_model": float(np.mean(reg <= 0.05)),
+            "regret_pruned3_mean": float(reg3.mean()), "within_5pct_pruned3": float(np.mean(reg3 <= 0.05)),
+            "regret_default_mean": float(regd.mean()), "within_5pct_default": float(np.mean(regd <= 0.05)),
+            "model_gflops_total": float(sum(5.0 * r["n"] * math.log2(r["n"]) * r["batch"] for r in res)
+                                        / sum(r["model_ms"] for r in res) / 1e6),
+            "best_gflops_total": float(sum(5.0 * r["n"] * math.log2(r["n"]) * r["batch"] for r in res)
+                                       / sum(r["best_ms"] for r in res) / 1e6),
+            "n_2pow27": big[0] if big else None}
+    print(json.dumps(line), flush=True)
+    if args.planner_out:
+        os.makedirs(args.planner_out, exist_ok=True)
+        tuner.save_table(rows, os.path.join(args.planner_out, "timings.json"))
+        with open(os.path.join(args.planner_out, "heldout.json"), "w") as f:
+            json.dump(res, f)
+        model.save(os.path.join(args.planner_out, "cost_model.npz"))
+
+
 def main():
     args = parse()
+    if args.planner:
+        run_planner(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -274,6 +274,22 @@ __device__ __forceinline__ void store_tile(const EngineArgs& a, const typename V
       if (a.conj) v = cconj(v);
       tile[i] = cscale(v, sc);
     }
+  } else if (a.gNs == 1) {
+    // first global pass: lane b's outputs are the L contiguous elements at
+    // t*N + b*L, and adjacent lanes are adjacent rows, so the tile's output
+    // is one contiguous run per transform: write it sample-fastest
+    const int W = a.W;
+    for (int i = threadIdx.x; i < W * L; i += blockDim.x) {
+      const int lane = (int)fdiv((unsigned)i, a.fd_L);
+      const int s = i - lane * L;
+      const long long u = u0 + lane;
+      if (u >= a.nunits) break;
+      const long long t = u / a.stride;
+      const long long b = u - t * a.stride;
+      V v = buf[lane * a.Lp + pad<T>(s)];
+      if (a.conj) v = cconj(v);
+      out[t * a.N + b * L + s] = cscale(v, sc);
+    }
   } else {
     const int W = a.W;
     const int lane = threadIdx.x % W;

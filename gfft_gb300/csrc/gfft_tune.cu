@@ -54,14 +54,17 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   const int variants[] = {0, 1};
   const int caps[] = {0, 256, 64};
   struct K {
-    int cap, v, mr, ro, st;
+    int cap, v, mr, ro, st, w;
   };
   std::vector<K> ks;
-  for (int st : {0, 1, 3}) ks.push_back({0, 0, 16, 0, st});
+  for (int st : {0, 1, 3}) ks.push_back({0, 0, 16, 0, st, 0});
+  // wider column tiles (128- and 256-byte rows) with shorter passes
+  for (int cap : {0, 512, 256, 128})
+    for (int w : {16, 32}) ks.push_back({cap, 0, 16, 0, 0, w});
   for (int cap : caps)
     for (int v : variants)
       for (int mr : radices)
-        for (int ro : orders) ks.push_back({cap, v, mr, ro, 0});
+        for (int ro : orders) ks.push_back({cap, v, mr, ro, 0, 0});
   for (const K& k : ks) {
     gfft_plan_opts o;
     std::memset(&o, 0, sizeof(o));
@@ -70,8 +73,14 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
     o.kernel_variant = k.v;
     o.stages = k.st;
     o.max_pass_len = k.cap;
+    o.units_per_block = k.w;
     gfft_plan_info info;
     if (gfft_plan_query(n, vtype_id, trans_id, place_id, batch, &o, &info) != GFFT_OK) continue;
+    if (k.w != 0) {  // a lane width only where the column-tile kernel runs
+      bool lanes = false;
+      for (int g = 0; g < info.n_global_passes; ++g) lanes |= (info.kernel_variant[g] == 4);
+      if (!lanes) continue;
+    }
     if (k.st != 0) {  // a depth variant only where a pipelined kernel runs
       bool pipelined = false;
       for (int g = 0; g < info.n_global_passes; ++g)

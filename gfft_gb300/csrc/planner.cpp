@@ -254,12 +254,16 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       }
     }
     // pipelined column tiles for the passes of a multi-pass length
-    if (gp.mode == 1 && (o.variant == 0 || o.variant == 4) && o.units == 0 && o.threads == 0) {
+    if (gp.mode == 1 && (o.variant == 0 || o.variant == 4) && o.threads == 0) {
       const long long TILE = dbl ? 2048 : 4096;
       const long long stride = n / gp.L;
       long long W = 1;
-      while (W * 2 * gp.L <= TILE && W * 2 <= stride && W * 2 <= 8) W *= 2;
-      if (W * gp.L <= TILE) {
+      if (o.units > 0) {  // requested lane width (a power of two), within 3 buffers of 64 KB
+        while (W * 2 <= o.units && W * 2 <= stride && 3 * W * 2 * padded(gp.L) * esz <= 200 * 1024) W *= 2;
+      } else {
+        while (W * 2 * gp.L <= TILE && W * 2 <= stride && W * 2 <= 8) W *= 2;
+      }
+      if (3 * W * padded(gp.L) * esz <= 200 * 1024) {
         gp.variant = 4;
         gp.units = (int)W;
         gp.threads = 256;
