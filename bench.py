@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--planner-train", type=int, default=150, help="training sizes (about 13 plans each)")
     p.add_argument("--planner-test", type=int, default=200, help="held-out sizes up to 2^27")
     p.add_argument("--planner-out", default="", help="directory for the timing table and model weights")
+    p.add_argument("--opts", default="", help="with --suite: plan options as JSON, e.g. '{\"kernel_variant\": 1}'")
     p.add_argument("--only", default="", help="with --suite: run the configurations whose name contains this")
     p.add_argument("--suite", action="store_true",
                    help="time every configuration of the workload list (one JSON line each) instead of the headline")
@@ -268,7 +269,7 @@ def run_suite(args):
         vt = G.DOUBLE if dbl else G.FLOAT
         tt = G.RDFT if tr == 2 else G.DFT
         place = G.IN_PLACE if pl == 0 else G.OUT_OF_PLACE
-        obj = G.TransformObject(n, vt, tt, 1, G.Serial, place, batch)
+        obj = G.TransformObject(n, vt, tt, 1, G.Serial, place, batch, json.loads(args.opts) if args.opts else None)
         info = obj.info()
 
         def step(o=obj):
