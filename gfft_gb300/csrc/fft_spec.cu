@@ -230,6 +230,145 @@ __global__ void __launch_bounds__(spec::Cfg<T>::TILE / 16, 1) spec_kernel(const 
   }
 }
 
+
+// ---- power-of-two column tiles of a multi-pass length (variant 5) --------
+// The passes of spec_kernel, for the W = tile / L adjacent lanes of a global
+// pass (plan.h): the next tile is gathered with 8/16-byte cp.async copies
+// into the second of two padded buffers while the current one is
+// transformed; each thread conjugates / applies the four-step twiddle to the
+// elements it gathered, the in-block passes run in place with their legs in
+// registers, and the result is stored either straight from registers (first
+// global pass: each lane's outputs are contiguous) or, through the buffer,
+// lane-fastest with stride Ns (later passes).
+namespace lanep2 {
+
+__device__ __forceinline__ uint32_t sa(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+template <typename T> __device__ __forceinline__ void cpa(uint32_t dst, const void* src);
+template <> __device__ __forceinline__ void cpa<float>(uint32_t dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+template <> __device__ __forceinline__ void cpa<double>(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+template <typename T, int L>
+__device__ __forceinline__ void gather(const EngineArgs& a, typename Vec<T>::t* buf, long long tile) {
+  typedef typename Vec<T>::t V;
+  constexpr int W = spec::Cfg<T>::TILE / L, NT = spec::Cfg<T>::TILE / 16, LP = L + (L >> spec::Cfg<T>::PS) + 1;
+  const int lane = threadIdx.x % W;
+  const long long u = tile * W + lane;
+  if (u >= a.nunits) return;
+  const long long t = u / a.stride;
+  const long long b = u - t * a.stride;
+  const V* src = (const V*)a.in + t * a.N + b;
+  V* bl = buf + lane * LP;
+  for (int s = threadIdx.x / W; s < L; s += NT / W)
+    cpa<T>(sa(bl + spec::padi<T>(s)), src + (long long)s * a.stride);
+}
+
+template <typename T, int L>
+__device__ __forceinline__ void sweep(const EngineArgs& a, typename Vec<T>::t* buf, long long tile) {
+  typedef typename Vec<T>::t V;
+  constexpr int W = spec::Cfg<T>::TILE / L, NT = spec::Cfg<T>::TILE / 16, LP = L + (L >> spec::Cfg<T>::PS) + 1;
+  const int lane = threadIdx.x % W;
+  const long long u = tile * W + lane;
+  const unsigned b = (unsigned)(u % a.stride);
+  const unsigned k = b % (unsigned)a.gNs;
+  const unsigned kstep = k * (unsigned)(a.N / (a.gNs * L));
+  if (!kstep && !a.conj) return;
+  V* bl = buf + lane * LP;
+  const V* lo = (const V*)a.gtw_lo;
+  const V* hi = (const V*)a.gtw_hi;
+  const unsigned mask = (unsigned)a.gB - 1;
+  const int lgB = 31 - __clz((int)a.gB);
+  for (int s = threadIdx.x / W; s < L; s += NT / W) {
+    V x = bl[spec::padi<T>(s)];
+    if (a.conj) x = cconj(x);
+    if (kstep) {
+      const unsigned m = kstep * (unsigned)s;  // < N < 2^32
+      x = cmul(x, cmul(__ldg(lo + (m & mask)), __ldg(hi + (m >> lgB))));
+    }
+    bl[spec::padi<T>(s)] = x;
+  }
+}
+
+template <typename T, int L, int P>
+__device__ __forceinline__ void passes(typename Vec<T>::t (&v)[16], typename Vec<T>::t* buf,
+                                       const typename Vec<T>::t* tw, const BlockPass* bp) {
+  constexpr int NP = spec::npass_of(L);
+  if constexpr (P < NP) {
+    spec::sread<T, L, P, false>(v, buf);
+    spec::scompute<T, L, P>(v, tw, bp[P].tw);
+    if constexpr (P < NP - 1) {
+      __syncthreads();
+      spec::swrite<T, L, P>(v, buf);
+      __syncthreads();
+      passes<T, L, P + 1>(v, buf, tw, bp);
+    }
+  }
+}
+
+}  // namespace lanep2
+
+template <typename T, int L>
+__global__ void __launch_bounds__(spec::Cfg<T>::TILE / 16, 2) lanep2_kernel(const __grid_constant__ EngineArgs a) {
+  typedef typename Vec<T>::t V;
+  constexpr int TILE = spec::Cfg<T>::TILE, W = TILE / L, NP = spec::npass_of(L), NT = TILE / 16;
+  constexpr int LP = L + (L >> spec::Cfg<T>::PS) + 1;
+  constexpr int NB = L / spec::radix_of(L, NP - 1);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* const bufs0 = reinterpret_cast<V*>(smem_raw);
+  V* const bufs1 = bufs0 + W * LP;
+  const V* tw = (const V*)a.tw;
+  const long long G = gridDim.x;
+  const T sc = (T)a.scale;
+  long long tile = blockIdx.x;
+  if (tile >= a.ntiles) return;
+  lanep2::gather<T, L>(a, bufs0, tile);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  V v[16];
+  for (int it = 0; tile < a.ntiles; tile += G, ++it) {
+    V* cur = (it & 1) ? bufs1 : bufs0;
+    V* nxt = (it & 1) ? bufs0 : bufs1;
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    lanep2::sweep<T, L>(a, cur, tile);
+    __syncthreads();
+    if (tile + G < a.ntiles) lanep2::gather<T, L>(a, nxt, tile + G);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    lanep2::passes<T, L, 0>(v, cur, tw, a.pass);
+    // v holds the last pass: thread's butterflies b = tid + q*NT, lane = b / NB, j = b % NB,
+    // leg r is sample j + r*NB of that lane
+    const long long u0 = tile * W;
+    const long long t = u0 / a.stride;
+    const long long b0 = u0 - t * a.stride;
+    const int units = (int)((a.nunits - u0) < W ? (a.nunits - u0) : W);
+    if (a.gNs == 1) {
+      spec::sstore<T, L, NP - 1>(v, (V*)a.out + t * a.N + b0 * L, units, a.conj != 0, sc);
+    } else {
+      __syncthreads();
+      spec::swrite<T, L, NP - 1>(v, cur);  // last pass: Ns*R == L, natural order
+      __syncthreads();
+      const int lane = threadIdx.x % W;
+      const long long u = u0 + lane;
+      if (u < a.nunits) {
+        const long long tt = u / a.stride;
+        const long long b = u - tt * a.stride;
+        const long long k = b % a.gNs;
+        V* dst = (V*)a.out + tt * a.N + (b - k) * L + k;
+        const V* bl = cur + lane * LP;
+        for (int s = threadIdx.x / W; s < L; s += NT / W) {
+          V x = bl[spec::padi<T>(s)];
+          if (a.conj) x = cconj(x);
+          dst[(long long)s * a.gNs] = cscale(x, sc);
+        }
+      }
+    }
+    (void)NB;
+    __syncthreads();
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 }  // namespace gfft
 
 namespace {
@@ -294,6 +433,46 @@ extern "C" int gfft_spec_launch(int dbl, const EngineArgs* a, unsigned grid, uns
                                 cudaStream_t stream) {
   const void* f = dbl ? spec_fn<double>(a->L) : spec_fn<float>(a->L);
   if (!f) return (int)cudaErrorInvalidValue;
+  void* args[] = {(void*)a};
+  return (int)cudaLaunchKernel(f, dim3(grid), dim3(threads), args, smem, stream);
+}
+
+namespace {
+template <typename T>
+const void* lanep2_fn(int L) {
+  switch (L) {
+    case 64: return (const void*)gfft::lanep2_kernel<T, 64>;
+    case 128: return (const void*)gfft::lanep2_kernel<T, 128>;
+    case 256: return (const void*)gfft::lanep2_kernel<T, 256>;
+    case 512: return (const void*)gfft::lanep2_kernel<T, 512>;
+    case 1024: return (const void*)gfft::lanep2_kernel<T, 1024>;
+    default: return nullptr;
+  }
+}
+}  // namespace
+
+extern "C" int gfft_lanep2_setup(int dbl, size_t max_smem) {
+  int e = 0;
+  for (int L : {64, 128, 256, 512, 1024}) {
+    const void* f = dbl ? lanep2_fn<double>(L) : lanep2_fn<float>(L);
+    e |= cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem) != cudaSuccess;
+  }
+  return e;
+}
+
+extern "C" int gfft_lanep2_occupancy(int dbl, int L, int threads, size_t smem) {
+  const void* f = dbl ? lanep2_fn<double>(L) : lanep2_fn<float>(L);
+  if (!f) return 0;
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem);
+  return n;
+}
+
+extern "C" int gfft_lanep2_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                  cudaStream_t stream) {
+  const void* f = dbl ? lanep2_fn<double>(a->L) : lanep2_fn<float>(a->L);
+  if (!f) return (int)cudaErrorInvalidValue;
+  cudaGetLastError();  // clear a stale error of an earlier, unrelated call
   void* args[] = {(void*)a};
   return (int)cudaLaunchKernel(f, dim3(grid), dim3(threads), args, smem, stream);
 }

@@ -61,6 +61,8 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   // wider column tiles (128- and 256-byte rows) with shorter passes
   for (int cap : {0, 512, 256, 128})
     for (int w : {16, 32}) ks.push_back({cap, 0, 16, 0, 0, w});
+  // the prefetching column tiles where the specialised ones are the default
+  for (int cap : caps) ks.push_back({cap, 4, 16, 0, 0, 0});
   for (int cap : caps)
     for (int v : variants)
       for (int mr : radices)

@@ -271,8 +271,37 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.smem = (size_t)(3 * W * padded(gp.L) * esz);  // prefetch buffer + ping-pong pair
       }
     }
-    // length-specialised variant: default radix order, L in the compiled set
+    // column tiles with the length-specialised passes: power-of-two L in
+    // 64..1024 with the default radix order; every tile of W = tile / L lanes
+    // lies inside one transform (n a multiple of the tile) and the twiddle
+    // exponents fit 32 bits
     const long long TILE = dbl ? 2048 : 4096;
+    if (gp.mode == 1 && (o.variant == 0 || o.variant == 5) && o.threads == 0 && o.units == 0 &&
+        o.radix_order == 0 && o.max_radix == 16 && gp.L >= 64 && gp.L <= 1024 && (gp.L & (gp.L - 1)) == 0 &&
+        n % TILE == 0 && n < (1LL << 31)) {
+      // the in-block radices must be the specialised kernel's: radix 16 while
+      // four bits remain, the remainder as 8 x 4 (one bit), 4 or 8
+      int lg = 0;
+      while ((1LL << lg) < gp.L) ++lg;
+      std::vector<int> want((std::size_t)(lg / 4), 16);
+      if (lg % 4 == 1) {
+        want.back() = 8;
+        want.push_back(4);
+      } else if (lg % 4) {
+        want.push_back(1 << (lg % 4));
+      }
+      bool ok = (int)want.size() == gp.npass;
+      for (int i = 0; i < gp.npass && ok; ++i) ok = gp.pass[i].R == want[(std::size_t)i];
+      if (ok) {
+        const long long W = TILE / gp.L;
+        gp.variant = 5;
+        gp.units = (int)W;
+        gp.threads = (int)(TILE / 16);
+        gp.ntiles = (batch * (n / gp.L)) / W;
+        gp.smem = (size_t)(2 * W * padded(gp.L) * esz);  // current tile + the next one's gather
+      }
+    }
+    // length-specialised variant: default radix order, L in the compiled set
     bool spec = gp.variant == 2 && (o.variant == 0 || o.variant == 3) && o.units == 0 && o.threads == 0 &&
                 gp.L <= TILE && o.radix_order == 0 && o.max_radix == 16;
     if (spec) {

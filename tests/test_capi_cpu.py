@@ -73,6 +73,25 @@ def test_plan_power_of_two_uses_radix16():
     assert d["radices"] == [[4] * 6]
 
 
+def test_plan_column_kernel_selection():
+    """Power-of-two passes of 64..1024 take the length-specialised column
+    tiles (5); other lengths, explicit options and short transforms keep the
+    prefetching column tiles (4)."""
+    for n, vt in ((1 << 16, 1), (1 << 20, 1), (1 << 24, 1), (1 << 20, 0), (1 << 22, 0)):
+        d = _lib.plan_query(n, vt, 0, 1, 1)
+        assert d["n_global_passes"] >= 2 and set(d["kernel_variant"]) == {5}, (n, vt, d)
+        assert all(64 <= L <= 1024 for L in d["pass_len"])
+    assert set(_lib.plan_query(5 ** 8, 1, 0, 1, 1)["kernel_variant"]) == {4}
+    assert set(_lib.plan_query(1 << 20, 1, 0, 1, 1, {"kernel_variant": 4})["kernel_variant"]) == {4}
+    assert set(_lib.plan_query(1 << 20, 1, 0, 1, 1, {"max_radix": 8})["kernel_variant"]) == {4}
+    # an 8192-point FP64 transform of two 64 x 128 passes: tile (2048) divides n
+    d = _lib.plan_query(8192, 0, 0, 1, 1, {"max_pass_len": 128})
+    assert set(d["kernel_variant"]) == {5}, d
+    # 1024 points in two passes: a 2048-value tile would span transforms
+    d = _lib.plan_query(1024, 0, 0, 1, 4, {"max_pass_len": 64})
+    assert 5 not in d["kernel_variant"], d
+
+
 def test_plan_errors():
     with pytest.raises(_lib.GfftError) as e:
         _lib.plan_query(0, 0, 0, 1)

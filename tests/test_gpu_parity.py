@@ -442,6 +442,53 @@ def test_cpp_facade_on_gpu(cuda):
     assert "facade ok (gpu)" in r.stdout
 
 
+@pytest.mark.parametrize("n,dbl,B,cap", [(1 << 13, 0, 3, 1024), (1 << 16, 0, 2, 0), (1 << 20, 0, 1, 0),
+                                         (1 << 24, 0, 1, 0), (1 << 17, 0, 2, 64), (1 << 12, 1, 5, 64),
+                                         (1 << 18, 1, 2, 0), (1 << 22, 1, 1, 0), (1 << 15, 0, 3, 128)])
+def test_multipass_spec_columns(cuda, oracle, n, dbl, B, cap):
+    """The length-specialised column-tile kernel (variant 5, chosen by default
+    for power-of-two passes of 64..1024) against the generic engine and the
+    prefetching column-tile kernel, forward and inverse, out of place and in
+    place, and against the exact oracle."""
+    from gfft_gb300 import _lib
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    base = {"max_pass_len": cap} if cap else {}
+    info = _lib.plan_query(n, vt, 0, 1, B, base or None)
+    assert info["n_global_passes"] >= 2 and all(v == 5 for v in info["kernel_variant"]), info
+    x = inputs.gaussian(17 + n, 2 * n * B).astype(dt)
+    for tr in (0, 1):
+        spec = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts=base or None)
+        gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts=dict(base, kernel_variant=1))
+        lane = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts=dict(base, kernel_variant=4))
+        inp = run_gpu(cuda, n, vt, tr, 0, x, batch=B, opts=base or None)
+        assert rel(spec, gen) <= tol(n, dbl), (n, tr, rel(spec, gen))
+        assert rel(spec, lane) <= tol(n, dbl), (n, tr, rel(spec, lane))
+        assert np.array_equal(spec, inp), (n, tr)
+    if n <= 1 << 20:
+        for tr in (0, 1):
+            k = min(B, 2)
+            ex = oracle.fft_ld(x[:2 * n * k].astype(np.float64), n, k, 1 if tr == 0 else -1)
+            y = run_gpu(cuda, n, vt, tr, 1, x[:2 * n * k], batch=k, opts=base or None)
+            if tr == 1:
+                ex = ex / n
+            assert rel(y, ex) <= tol(n, dbl), (n, tr, rel(y, ex))
+
+
+@pytest.mark.parametrize("n,dbl", [(1 << 14, 0), (1 << 21, 0), (1 << 16, 1)])
+def test_multipass_spec_columns_real(cuda, n, dbl):
+    """Real transforms whose complex half-length runs through variant 5:
+    forward against numpy's FP64 real DFT in the packed layout, and the
+    inverse round trip."""
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    x = inputs.gaussian(5 + n, 2 * n).astype(dt)
+    y = run_gpu(cuda, n, vt, 2, 1, x)
+    assert rel(y, packed_rfft(x)) <= tol(2 * n, dbl)
+    z = run_gpu(cuda, n, vt, 3, 1, y)
+    assert rel(z, x) <= 2 * tol(2 * n, dbl)
+
+
 @pytest.mark.parametrize("n,dbl,B", [(786432, 0, 3), (390625, 1, 2), (248832, 0, 5), (1 << 20, 1, 1),
                                      (12288, 0, 7), (1 << 24, 0, 1), (3 * 5 * 7 * 11 * 13 * 16, 0, 1)])
 def test_multipass_pipelined_matches_engine(cuda, oracle, n, dbl, B):
