@@ -196,7 +196,7 @@ def run_reference(args):
 
 
 SUITE = [
-    # name, n, batch, dtype, trans (0 DFT, 2 RDFT), place, inputs, also time the inverse
+    # name, n, batch, dtype, trans (0 DFT, 2 RDFT), place, inputs, also time the inverse[, plan options]
     ("c1 fp64 c2c N=1024 x 4096 in place + ifft", 1024, 4096, "f64", 0, 0, "uniform", True),
     ("c2 fp32 c2c N=3*2^18 x 8", 3 * 2 ** 18, 8, "f32", 0, 1, "gaussian", False),
     ("c2 fp64 c2c N=3*2^18 x 8", 3 * 2 ** 18, 8, "f64", 0, 1, "gaussian", False),
@@ -205,8 +205,12 @@ SUITE = [
     ("c2 fp32 c2c N=2^10*3^5 x 8", 2 ** 10 * 3 ** 5, 8, "f32", 0, 1, "gaussian", False),
     ("c2 fp64 c2c N=2^10*3^5 x 8", 2 ** 10 * 3 ** 5, 8, "f64", 0, 1, "gaussian", False),
     ("c2b fp64 real N_real=2^20 x 16 in place", 2 ** 19, 16, "f64", 2, 0, "uniform", False),
-    ("c3 fp32 c2c N=4096 x 65536", 4096, 65536, "f32", 0, 1, "gaussian", False),
-    ("c3 fp32 c2c N=2^24 x 1", 2 ** 24, 1, "f32", 0, 1, "gaussian", False),
+    ("c3 fp32 c2c N=4096 x 65536", 4096, 65536, "f32", 0, 1, "gaussian+tones", False),
+    ("c3 fp32 c2c N=2^24 x 1", 2 ** 24, 1, "f32", 0, 1, "gaussian+tones", False),
+    ("c3 fp32 c2c N=4096 x 65536, tensor-core split", 4096, 65536, "f32", 0, 1, "gaussian+tones", False,
+     {"kernel_variant": 6}),
+    ("c3 fp32 c2c N=2^24 x 1, tensor-core split", 2 ** 24, 1, "f32", 0, 1, "gaussian+tones", False,
+     {"kernel_variant": 6}),
 ]
 
 
@@ -256,20 +260,25 @@ def run_suite(args):
     peak, _ = measured_peaks()
     if not args.only or args.only in "c4 ragged":
         run_ragged(args, peak)
-    for name, n, batch, dt, tr, pl, kind, inv in SUITE:
+    plain_ms = {}
+    for entry in SUITE:
+        name, n, batch, dt, tr, pl, kind, inv = entry[:8]
+        opts = entry[8] if len(entry) > 8 else (json.loads(args.opts) if args.opts else None)
         if args.only and args.only not in name:
             continue
         dbl = dt == "f64"
         tdt = torch.float64 if dbl else torch.float32
         nel = 2 * n * batch
-        gen = inputs.gaussian if kind == "gaussian" else inputs.uniform
+        gen = inputs.uniform if kind == "uniform" else inputs.gaussian
         xh = gen(0x5EED0000 + n, nel)
+        if kind == "gaussian+tones":  # 8 tones of amplitude 1e-4 on every transform
+            xh += inputs.tone_mix(0x5EED0003, n, batch)
         x = torch.from_numpy(xh).to(tdt).cuda()
         y = x.clone() if pl == 0 else torch.empty_like(x)
         vt = G.DOUBLE if dbl else G.FLOAT
         tt = G.RDFT if tr == 2 else G.DFT
         place = G.IN_PLACE if pl == 0 else G.OUT_OF_PLACE
-        obj = G.TransformObject(n, vt, tt, 1, G.Serial, place, batch, json.loads(args.opts) if args.opts else None)
+        obj = G.TransformObject(n, vt, tt, 1, G.Serial, place, batch, opts)
         info = obj.info()
 
         def step(o=obj):
@@ -295,7 +304,11 @@ def run_suite(args):
         line = {"config": name, "n": n, "batch": batch, "dtype": dt, "ms": ms, "GFLOP/s": fl / ms / 1e6,
                 "GB/s_algorithmic": alg_bytes / ms / 1e6, "frac_hbm": alg_bytes / ms / 1e6 / peak,
                 "passes": info["n_global_passes"], "radices": info["radices"], "variant": info["kernel_variant"],
-                "kernels_per_exec": info["kernels_per_exec"]}
+                "kernels_per_exec": info["kernels_per_exec"], "opts": opts or {}, "inputs": kind}
+        if not opts:
+            plain_ms[(n, batch, dt, tr)] = ms
+        elif (n, batch, dt, tr) in plain_ms:
+            line["speedup_vs_plain"] = plain_ms[(n, batch, dt, tr)] / ms
         if inv:
             invobj = obj.inverse_object()
             torch.cuda.synchronize()
@@ -308,7 +321,7 @@ def run_suite(args):
         # accuracy of one transform (fresh run) against numpy's FP64 FFT
         xs = torch.from_numpy(xh[:2 * n].copy()).to(tdt).cuda()
         ys = xs.clone() if pl == 0 else torch.empty_like(xs)
-        one = G.TransformObject(n, vt, tt, 1, G.Serial, place, 1)
+        one = G.TransformObject(n, vt, tt, 1, G.Serial, place, 1, opts)
         if pl == 0:
             one.fft(ys)
         else:

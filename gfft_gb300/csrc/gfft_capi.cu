@@ -37,6 +37,9 @@ extern "C" int gfft_lanep2_setup(int dbl, size_t max_smem);
 extern "C" int gfft_lanep2_occupancy(int dbl, int L, int threads, size_t smem);
 extern "C" int gfft_lanep2_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                   cudaStream_t stream);
+extern "C" int gfft_tc_setup(size_t max_smem);
+extern "C" int gfft_tc_occupancy(int L, int threads, size_t smem);
+extern "C" int gfft_tc_launch(const EngineArgs* a, unsigned grid, unsigned threads, size_t smem, cudaStream_t stream);
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
 
@@ -61,6 +64,7 @@ int setup_device_once(int dbl) {
   if (gfft_spec_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_lane_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_lanep2_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
+  if (!dbl && gfft_tc_setup((size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (dev < 64) done[dbl][dev] = true;
   return GFFT_OK;
 }
@@ -222,6 +226,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                     : (gp.variant == 3   ? gfft_spec_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 4 ? gfft_lane_occupancy(dbl, gp.threads, gp.smem)
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
+                       : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)
                                          : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
       if (per < 1) per = 1;
       long long grid = (long long)nsm * per;
@@ -391,6 +396,12 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     a.conj = inverse ? 1 : 0;
     a.scale = (inverse && last) ? 1.0 / (double)n : 1.0;
     a.status = h->d_status;
+    if (gp.variant == 6) {
+      a.ntiles = gp.ntiles;
+      a.spin_limit = 1LL << 26;
+      if (gfft_tc_launch(&a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      continue;
+    }
     if (gp.variant == 4 || gp.variant == 5) {
       a.ntiles = gp.ntiles;
       const int e = gp.variant == 4 ? gfft_lane_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream)

@@ -77,6 +77,25 @@ void wroot(long long j, long long m, double* re, double* im) {
   *im = (double)(-s);
 }
 
+// The in-block radices of the length-specialised kernels for a power-of-two
+// L: radix 16 while four bits remain, the remainder as 8 x 4 (one bit), 4 or
+// 8 (fft_spec.cu, spec.cuh radix_of).
+bool spec_radices(const GlobalPass& gp) {
+  int lg = 0;
+  while ((1LL << lg) < gp.L) ++lg;
+  if ((1LL << lg) != gp.L || lg < 4) return false;
+  std::vector<int> want((std::size_t)(lg / 4), 16);
+  if (lg % 4 == 1) {
+    want.back() = 8;
+    want.push_back(4);
+  } else if (lg % 4) {
+    want.push_back(1 << (lg % 4));
+  }
+  bool ok = (int)want.size() == gp.npass;
+  for (int i = 0; i < gp.npass && ok; ++i) ok = gp.pass[i].R == want[(std::size_t)i];
+  return ok;
+}
+
 std::vector<int> block_radices(int L, const PlanOpts& o) {
   std::vector<int> pow2, odd, gen;
   int a = 0;
@@ -279,20 +298,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     if (gp.mode == 1 && (o.variant == 0 || o.variant == 5) && o.threads == 0 && o.units == 0 &&
         o.radix_order == 0 && o.max_radix == 16 && gp.L >= 64 && gp.L <= 1024 && (gp.L & (gp.L - 1)) == 0 &&
         n % TILE == 0 && n < (1LL << 31)) {
-      // the in-block radices must be the specialised kernel's: radix 16 while
-      // four bits remain, the remainder as 8 x 4 (one bit), 4 or 8
-      int lg = 0;
-      while ((1LL << lg) < gp.L) ++lg;
-      std::vector<int> want((std::size_t)(lg / 4), 16);
-      if (lg % 4 == 1) {
-        want.back() = 8;
-        want.push_back(4);
-      } else if (lg % 4) {
-        want.push_back(1 << (lg % 4));
-      }
-      bool ok = (int)want.size() == gp.npass;
-      for (int i = 0; i < gp.npass && ok; ++i) ok = gp.pass[i].R == want[(std::size_t)i];
-      if (ok) {
+      if (spec_radices(gp)) {
         const long long W = TILE / gp.L;
         gp.variant = 5;
         gp.units = (int)W;
@@ -300,6 +306,20 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.ntiles = (batch * (n / gp.L)) / W;
         gp.smem = (size_t)(2 * W * padded(gp.L) * esz);  // current tile + the next one's gather
       }
+    }
+    // split-precision tensor-core form, on request: FP32 complex, power-of-two
+    // L in 64..4096 with the specialised radices (the radix-16 passes on the
+    // tensor cores); a multi-pass length must be a multiple of the tile
+    if (o.variant == 6 && !dbl && trans < 2 && o.threads == 0 && o.units == 0 && o.radix_order == 0 &&
+        o.max_radix == 16 && gp.L >= 64 && gp.L <= 4096 && (plan.nglobal == 1 || n % 4096 == 0) &&
+        n < (1LL << 31) && spec_radices(gp)) {
+      const long long W = 4096 / gp.L;
+      gp.variant = 6;
+      gp.units = (int)W;
+      gp.threads = 256;
+      gp.ntiles = (batch * (n / gp.L) + W - 1) / W;
+      // aligned operands (1 KB slack, 32 KB A, 4 KB B), two padded buffers, mbarrier and TMEM slot
+      gp.smem = (size_t)(1024 + 32768 + 4096 + 2 * W * padded(gp.L) * 8 + 16);
     }
     // length-specialised variant: default radix order, L in the compiled set
     bool spec = gp.variant == 2 && (o.variant == 0 || o.variant == 3) && o.units == 0 && o.threads == 0 &&

@@ -443,8 +443,8 @@ def test_cpp_facade_on_gpu(cuda):
 
 
 @pytest.mark.parametrize("n,dbl,B,cap", [(1 << 13, 0, 3, 1024), (1 << 16, 0, 2, 0), (1 << 20, 0, 1, 0),
-                                         (1 << 24, 0, 1, 0), (1 << 17, 0, 2, 64), (1 << 12, 1, 5, 64),
-                                         (1 << 18, 1, 2, 0), (1 << 22, 1, 1, 0), (1 << 15, 0, 3, 128)])
+                                         (1 << 24, 0, 1, 0), (1 << 18, 0, 2, 64), (1 << 12, 1, 5, 64),
+                                         (1 << 18, 1, 2, 0), (1 << 22, 1, 1, 0), (1 << 15, 0, 3, 256)])
 def test_multipass_spec_columns(cuda, oracle, n, dbl, B, cap):
     """The length-specialised column-tile kernel (variant 5, chosen by default
     for power-of-two passes of 64..1024) against the generic engine and the
