@@ -10,12 +10,15 @@
 //     to the 32 reals of a butterfly.  The 256 butterflies of a 4096-value
 //     tile form D (256 x 32) = X (256 x 32) F^T: two M = 128, N = 32 products;
 //   - operands are FP16 pairs x = x_hi + x_lo (x_lo = fp16(x - x_hi)) and
-//     likewise F; D = X_hi F_hi + X_lo F_hi + X_hi F_lo (the x_lo F_lo term,
-//     ~2^-22 relative, is dropped) accumulated in FP32 in tensor memory;
+//     likewise F; D = X_hi F_hi + (X_lo F_hi + X_hi F_lo) (the x_lo F_lo
+//     term, ~2^-24 relative, is dropped): the main product and the two
+//     correction products in separate FP32 accumulators in tensor memory,
+//     added on the CUDA cores (round to nearest), so the accumulator
+//     roundings of the correction chain fall on values 2^-11 smaller;
 //   - every butterfly row is scaled by a power of two that brings its largest
-//     component to [1, 2) before the split (no FP16 overflow as values grow
-//     pass to pass, small components keep FP16's relative precision) and is
-//     unscaled exactly after;
+//     component to [2^14, 2^15) before the split (no FP16 overflow as values
+//     grow pass to pass; components down to 2^-28 of the row's largest stay
+//     normal FP16 numbers) and is unscaled exactly after;
 //   - the inter-pass and four-step twiddles are applied in FP32 on the CUDA
 //     cores before the split; passes of radix 8 / 4 / 2 run on the CUDA cores.
 //
@@ -24,10 +27,11 @@
 // logical chunk c of row m sits at chunk c ^ (m % 8); 8-row atoms of 1024
 // bytes, 1024-aligned.  The K = 16 steps of one product start 32 bytes apart
 // inside the row.  One thread (thread 0) issues the 12 MMAs of a pass and a
-// commit that arrives on an mbarrier; the accumulator (2 x 32 TMEM columns)
-// is read back with 32x32b loads: warp w reads lanes 32 (w % 4) .. + 31 of
-// M-tile w / 4, which are the rows thread 32 w + lane converted, so each
-// thread unscales its own butterfly with the scale it kept in a register.
+// commit that arrives on an mbarrier; the accumulators (2 x 2 x 32 TMEM
+// columns) are read back with 32x32b loads: warp w reads lanes 32 (w % 4) ..
+// + 31 of M-tile w / 4, which are the rows thread 32 w + lane converted, so
+// each thread unscales its own butterfly with the scale it kept in a
+// register.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -43,7 +47,7 @@ namespace tc {
 constexpr int TILE = 4096, NT = 256;
 constexpr int A_BYTES = 2 * 128 * 128;  // two M-tiles x 128 rows x 128 bytes
 constexpr int B_BYTES = 32 * 128;       // 32 rows (outputs) x 128 bytes
-constexpr int TMEM_COLS = 64;           // 2 M-tiles x N = 32 FP32 columns
+constexpr int TMEM_COLS = 128;          // main and correction accumulators, 2 M-tiles x N = 32 each
 
 // cos(2 pi m / 16)
 __constant__ float kCos16[16] = {1.0f,
@@ -127,10 +131,11 @@ __device__ __forceinline__ float split_row(const float2 (&v)[16], unsigned char*
   float mx = 0.f;
 #pragma unroll
   for (int i = 0; i < 16; ++i) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
+  // mx in [2^(e-127), 2^(e-126)): scale by 2^(141-e) into [2^14, 2^15)
   int e = (int)((__float_as_uint(mx) >> 23) & 0xFFu);
-  e = e < 1 ? 1 : (e > 253 ? 253 : e);
-  const float s = __uint_as_float((uint32_t)(254 - e) << 23);  // 2^(127 - e)
-  const float inv = __uint_as_float((uint32_t)e << 23);        // 2^(e - 127)
+  e = e < 15 ? 15 : (e > 254 ? 254 : e);
+  const float s = __uint_as_float((uint32_t)(268 - e) << 23);   // 2^(141 - e)
+  const float inv = __uint_as_float((uint32_t)(e - 14) << 23);  // 2^(e - 141)
   unsigned char* row = A + (t >> 7) * 16384 + ((t & 127) >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
@@ -167,14 +172,15 @@ __device__ __forceinline__ bool dft16(float2 (&v)[16], Ctx& c) {
     fence_after();
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
-      const uint32_t d = c.tmem + 32 * mt;
+      const uint32_t d = c.tmem + 32 * mt;        // main accumulator
+      const uint32_t dc = c.tmem + 64 + 32 * mt;  // correction accumulator
       const uint32_t am = c.a_s + mt * 16384;
       mma(d, sdesc(am + 0), sdesc(c.b_s + 0), 0);    // x_hi F_hi, k 0..15
       mma(d, sdesc(am + 32), sdesc(c.b_s + 32), 1);  // x_hi F_hi, k 16..31
-      mma(d, sdesc(am + 64), sdesc(c.b_s + 0), 1);   // x_lo F_hi
-      mma(d, sdesc(am + 96), sdesc(c.b_s + 32), 1);
-      mma(d, sdesc(am + 0), sdesc(c.b_s + 64), 1);   // x_hi F_lo
-      mma(d, sdesc(am + 32), sdesc(c.b_s + 96), 1);
+      mma(dc, sdesc(am + 64), sdesc(c.b_s + 0), 0);  // x_lo F_hi
+      mma(dc, sdesc(am + 96), sdesc(c.b_s + 32), 1);
+      mma(dc, sdesc(am + 0), sdesc(c.b_s + 64), 1);  // x_hi F_lo
+      mma(dc, sdesc(am + 32), sdesc(c.b_s + 96), 1);
     }
     commit(c.bar);
   }
@@ -186,10 +192,15 @@ __device__ __forceinline__ bool dft16(float2 (&v)[16], Ctx& c) {
   c.phase ^= 1u;
   fence_after();
   const int w = threadIdx.x >> 5;
+  const uint32_t ta = c.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(32 * (w >> 2));
   uint32_t r[32];
-  tmem_ld32(c.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(32 * (w >> 2)), r);
+  tmem_ld32(ta, r);
 #pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = make_float2(__uint_as_float(r[2 * i]) * inv, __uint_as_float(r[2 * i + 1]) * inv);
+  for (int i = 0; i < 16; ++i) v[i] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+  tmem_ld32(ta + 64, r);
+#pragma unroll
+  for (int i = 0; i < 16; ++i)
+    v[i] = make_float2((v[i].x + __uint_as_float(r[2 * i])) * inv, (v[i].y + __uint_as_float(r[2 * i + 1])) * inv);
   fence_before();  // the loads precede the next pass's MMAs across the next barrier
   return true;
 }

@@ -56,6 +56,8 @@ def test_tc_split_vs_oracle(cuda, oracle, n, batch):
     y = run(cuda, n, 0, 1, x, batch, TC)
     e_tc = rel(y[:2 * n * k], ex)
     e_plain = rel(run(cuda, n, 0, 1, x[:2 * n * k], k), ex)
+    print("tc-split n=%d batch=%d rel_l2 tc %.3e plain %.3e max_abs tc %.3e" %
+          (n, batch, e_tc, e_plain, np.max(np.abs(y[:2 * n * k] - ex))))
     assert e_tc <= TOL_TC, (n, e_tc, e_plain)
     # inverse (with its 1/N) and in place
     exi = oracle.fft_ld(x[:2 * n * k].astype(np.float64), n, k, -1)
