@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--planner-out", default="", help="directory for the timing table and model weights")
     p.add_argument("--opts", default="", help="with --suite: plan options as JSON, e.g. '{\"kernel_variant\": 1}'")
     p.add_argument("--only", default="", help="with --suite: run the configurations whose name contains this")
+    p.add_argument("--case", action="store_true",
+                   help="one FP32 C2C transform of --n x --batch with --opts, --warmup + --steps launches, device "
+                        "buffers only (small profiling runs)")
     p.add_argument("--suite", action="store_true",
                    help="time every configuration of the workload list (one JSON line each) instead of the headline")
     return p.parse_args()
@@ -461,8 +464,39 @@ def run_planner(args):
         model.save(os.path.join(args.planner_out, "cost_model.npz"))
 
 
+def run_case(args):
+    """--case: a plain timing loop over one plan, for profiler captures."""
+    import torch
+
+    import gfft_gb300
+    from gfft_gb300 import gfft as G
+    gfft_gb300.build()
+    n, batch = args.n, args.batch
+    opts = json.loads(args.opts) if args.opts else None
+    x = torch.rand(2 * n * batch, device="cuda", dtype=torch.float32)
+    y = torch.empty_like(x)
+    obj = G.TransformObject(n, G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, batch, opts)
+    for _ in range(args.warmup):
+        obj.fft(x, y)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        obj.fft(x, y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    info = obj.info()
+    print(json.dumps({"case": "fp32 c2c", "n": n, "batch": batch, "opts": opts or {}, "ms": ms,
+                      "GFLOP/s": flops(n, batch) / ms / 1e6, "variant": info["kernel_variant"],
+                      "pass_len": info["pass_len"]}))
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args)
+        return
     if args.planner:
         run_planner(args)
         return

@@ -34,16 +34,20 @@
 
 namespace gfft {
 
+// resident blocks per SM the register budget is sized for (70 KB of shared
+// memory per block)
+template <typename T> struct RaggedOcc { static constexpr int v = sizeof(T) == 4 ? 3 : 2; };
+
 template <typename T>
-__global__ void __launch_bounds__(256) ragged_kernel(const __grid_constant__ RaggedArgs ra) {
+__global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __grid_constant__ RaggedArgs ra) {
   typedef typename Vec<T>::t V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ EngineArgs ea;
-  __shared__ long long item_s;
+  __shared__ long long item_s, u0_s;
   __shared__ int abort_s;
   V* b0 = reinterpret_cast<V*>(smem_raw);
   V* b1 = b0 + ra.lanes_max;
-  const V* tab = (const V*)ra.tab;
+  int key = -1;  // (plan, pass) whose arguments `ea` holds
   while (true) {
     if (threadIdx.x == 0) {
       item_s = atomicAdd(ra.head, 1);
@@ -52,89 +56,69 @@ __global__ void __launch_bounds__(256) ragged_kernel(const __grid_constant__ Rag
     __syncthreads();
     const long long it = item_s;
     if (it >= ra.nitems) return;
+    const RaggedItem item = ra.items[it];
+    const int k = item.plan * GFFT_MAXG + item.pass;
+    if (k != key) {  // the engine arguments of this (plan, pass), copied by the whole block
+      const int* src = reinterpret_cast<const int*>(ra.ea + k);
+      int* dst = reinterpret_cast<int*>(&ea);
+      for (int w = threadIdx.x; w < (int)(sizeof(EngineArgs) / sizeof(int)); w += blockDim.x) dst[w] = __ldg(src + w);
+      key = k;
+      __syncthreads();
+    }
     if (threadIdx.x == 0) {
-      const RaggedItem item = ra.items[it];
       const RaggedPlan& pl = ra.plans[item.plan];
       const int g = item.pass;
       if (g > 0) {  // wait for every tile of the previous pass of this transform
         volatile int* d = ra.done + (long long)item.transform * GFFT_MAXG + (g - 1);
+        const int need = pl.tiles[g - 1];
         long long i = 0;
-        while (*d < pl.tiles[g - 1] && i < ra.spin_limit) {
+        while (*d < need && i < ra.spin_limit) {
           __nanosleep(64);
           ++i;
         }
-        if (*d < pl.tiles[g - 1]) {
+        if (*d < need) {
           atomicExch(ra.status, 13 /* GFFT_E_TIMEOUT */);
           abort_s = 1;
         }
         __threadfence();
       }
-      const int L = pl.L[g];
-      const int ps = sizeof(T) == 8 ? 3 : 4;
-      ea.L = L;
-      ea.Lp = L + (L >> ps) + 1;
-      ea.pad_shift = ps;
-      ea.N = pl.n;
-      ea.npass = pl.npass[g];
-      for (int i = 0; i < ea.npass; ++i) {
-        ea.pass[i] = pl.pass[g][i];
-        ea.pass[i].fd_nb = make_fastdiv((unsigned)(L / ea.pass[i].R));
-        ea.pass[i].fd_ns = make_fastdiv((unsigned)ea.pass[i].Ns);
-      }
-      ea.fd_L = make_fastdiv((unsigned)L);
-      ea.tw = tab + pl.tab;
-      ea.gtw_lo = tab + pl.tab + pl.gtw_lo;
-      ea.gtw_hi = tab + pl.tab + pl.gtw_hi;
-      ea.gB = pl.gB;
-      ea.conj = ra.conj;
-      ea.real = 0;
-      const bool last = (g == pl.nglobal - 1);
-      ea.scale = (ra.conj && last) ? 1.0 / (double)pl.n : 1.0;
-      ea.ldcg = g > 0;
       if (pl.nglobal == 1) {
-        ea.mode = 2;
         ea.in = ra.in;
         ea.out = ra.out;
         ea.lane_off = ra.lane_off + item.group;
         ea.W = item.count;
         ea.nunits = item.count;
-        ea.stride = 1;
-        ea.gNs = 1;
+        u0_s = 0;
       } else {
         // buffer chain: 2 passes in -> ws -> out; 3 passes in -> ws -> ws2 -> out
         const long long off = ra.offset[item.transform];
+        const bool last = (g == pl.nglobal - 1);
         const V* bufs_in[3] = {(const V*)ra.in, (const V*)ra.ws, (const V*)ra.ws + ra.ws2_off};
         V* bufs_out[3] = {(V*)ra.ws, (V*)ra.ws + ra.ws2_off, (V*)ra.out};
-        const V* src = bufs_in[g] + off;
-        V* dst = last ? (V*)ra.out + off : bufs_out[g] + off;
-        ea.mode = 1;
-        ea.in = src;
-        ea.out = dst;
-        ea.W = pl.W[g];
-        ea.stride = pl.n / L;
-        ea.nunits = ea.stride;
-        ea.gNs = pl.Ns[g];
+        ea.in = bufs_in[g] + off;
+        ea.out = last ? (V*)ra.out + off : bufs_out[g] + off;
+        u0_s = item.unit0;
       }
-      item_s = (pl.nglobal == 1) ? 0 : item.unit0;
     }
     __syncthreads();
     if (abort_s) return;
-    const long long u0 = item_s;
+    const long long u0 = u0_s;
     load_tile<T>(ea, b0, u0);
     __syncthreads();
     V* src = b0;
     V* dst = b1;
+    const V* tw = (const V*)ea.tw;
     for (int p = 0; p < ea.npass; ++p) {
       const BlockPass bp = ea.pass[p];
       switch (bp.R) {
-        case 16: block_pass<T, 16>(src, dst, ea, bp, (const V*)ea.tw); break;
-        case 8: block_pass<T, 8>(src, dst, ea, bp, (const V*)ea.tw); break;
-        case 4: block_pass<T, 4>(src, dst, ea, bp, (const V*)ea.tw); break;
-        case 2: block_pass<T, 2>(src, dst, ea, bp, (const V*)ea.tw); break;
-        case 3: block_pass<T, 3>(src, dst, ea, bp, (const V*)ea.tw); break;
-        case 5: block_pass<T, 5>(src, dst, ea, bp, (const V*)ea.tw); break;
-        case 7: block_pass<T, 7>(src, dst, ea, bp, (const V*)ea.tw); break;
-        default: block_pass_generic<T>(src, dst, ea, bp, (const V*)ea.tw); break;
+        case 16: block_pass<T, 16>(src, dst, ea, bp, tw); break;
+        case 8: block_pass<T, 8>(src, dst, ea, bp, tw); break;
+        case 4: block_pass<T, 4>(src, dst, ea, bp, tw); break;
+        case 2: block_pass<T, 2>(src, dst, ea, bp, tw); break;
+        case 3: block_pass<T, 3>(src, dst, ea, bp, tw); break;
+        case 5: block_pass<T, 5>(src, dst, ea, bp, tw); break;
+        case 7: block_pass<T, 7>(src, dst, ea, bp, tw); break;
+        default: block_pass_generic<T>(src, dst, ea, bp, tw); break;
       }
       __syncthreads();
       V* t = src;
@@ -144,13 +128,8 @@ __global__ void __launch_bounds__(256) ragged_kernel(const __grid_constant__ Rag
     store_tile<T>(ea, src, u0);
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) {
-      const RaggedItem& item = ra.items[it];
-      const RaggedPlan& pl = ra.plans[item.plan];
-      if (pl.nglobal > 1 && item.pass < pl.nglobal - 1)
-        atomicAdd(ra.done + (long long)item.transform * GFFT_MAXG + item.pass, 1);
-    }
-    __syncthreads();
+    if (threadIdx.x == 0 && ea.mode == 1 && item.pass < ra.plans[item.plan].nglobal - 1)
+      atomicAdd(ra.done + (long long)item.transform * GFFT_MAXG + item.pass, 1);
   }
 }
 
@@ -164,6 +143,7 @@ struct gfft_ragged {
   void* d_tab = nullptr;
   RaggedPlan* d_plans = nullptr;
   RaggedItem* d_items = nullptr;
+  EngineArgs* d_ea = nullptr;
   long long* d_lane_off = nullptr;
   long long* d_offset = nullptr;
   int* d_done = nullptr;
@@ -192,8 +172,8 @@ void free_ragged(gfft_ragged* r) {
   if (r->gexec) cudaGraphExecDestroy(r->gexec);
   if (r->graph) cudaGraphDestroy(r->graph);
   if (r->cap_stream) cudaStreamDestroy(r->cap_stream);
-  void* ps[] = {r->d_tab, r->d_plans, r->d_items, r->d_lane_off, r->d_offset, r->d_done, r->d_head, r->d_status,
-                r->d_ws};
+  void* ps[] = {r->d_tab, r->d_plans, r->d_items, r->d_ea, r->d_lane_off, r->d_offset, r->d_done, r->d_head,
+                r->d_status, r->d_ws};
   for (void* p : ps)
     if (p) cudaFree(p);
   delete r;
@@ -248,6 +228,8 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
   po.max_single = r->dbl ? 2048 : 4096;
   po.smem_budget = 72 * 1024;
   po.variant = 1;
+  po.units = r->dbl ? 2 : 4;  // sizes the pass-length cap: passes up to 1024 within the budget
+  const long long TILE = r->dbl ? 2048 : 4096;  // points per work item
   std::vector<RaggedPlan> plans(distinct.size());
   std::vector<double> tab;
   int lanes_max = 0;
@@ -274,8 +256,12 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
         while (W > 1 && 2LL * W * (gp.L + (gp.L >> ps) + 1) * esz > po.smem_budget) --W;
         rp.W[g] = W;
       } else {
-        rp.W[g] = gp.units;
-        rp.tiles[g] = (int)((distinct[d] / gp.L + gp.units - 1) / gp.units);
+        // columns per item: a power of two, about TILE points, within the transform
+        const long long stride = distinct[d] / gp.L;
+        long long W = 1;
+        while (2 * W * gp.L <= TILE && 2 * W <= stride && 2 * W <= 256) W *= 2;
+        rp.W[g] = (int)W;
+        rp.tiles[g] = (int)((stride + W - 1) / W);
       }
       lanes_max = std::max<int>(lanes_max, rp.W[g] * (gp.L + (gp.L >> ps) + 1));
     }
@@ -345,6 +331,50 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
   }
   if (st == GFFT_OK) st = upload((void**)&r->d_plans, plans);
   if (st == GFFT_OK) st = upload((void**)&r->d_items, items);
+  if (st == GFFT_OK) {
+    // engine arguments per (plan, global pass); the buffers are set per item
+    std::vector<EngineArgs> eas((size_t)r->nplans * GFFT_MAXG);
+    std::memset(eas.data(), 0, eas.size() * sizeof(EngineArgs));
+    const char* tb = (const char*)r->d_tab;
+    for (int d = 0; d < r->nplans; ++d) {
+      const RaggedPlan& pl = plans[(size_t)d];
+      for (int g = 0; g < pl.nglobal; ++g) {
+        EngineArgs& e = eas[(size_t)d * GFFT_MAXG + g];
+        const int L = pl.L[g];
+        e.L = L;
+        e.pad_shift = ps;
+        e.Lp = L + (L >> ps) + 1;
+        e.N = pl.n;
+        e.npass = pl.npass[g];
+        for (int i = 0; i < e.npass; ++i) {
+          e.pass[i] = pl.pass[g][i];
+          e.pass[i].fd_nb = make_fastdiv((unsigned)(L / e.pass[i].R));
+          e.pass[i].fd_ns = make_fastdiv((unsigned)e.pass[i].Ns);
+        }
+        e.fd_L = make_fastdiv((unsigned)L);
+        e.tw = tb + (size_t)pl.tab * esz;
+        e.gtw_lo = tb + (size_t)(pl.tab + pl.gtw_lo) * esz;
+        e.gtw_hi = tb + (size_t)(pl.tab + pl.gtw_hi) * esz;
+        e.gB = pl.gB;
+        e.conj = r->inverse;
+        e.real = 0;
+        e.scale = (r->inverse && g == pl.nglobal - 1) ? 1.0 / (double)pl.n : 1.0;
+        e.ldcg = g > 0;
+        if (pl.nglobal == 1) {
+          e.mode = 2;
+          e.stride = 1;
+          e.gNs = 1;
+        } else {
+          e.mode = 1;
+          e.W = pl.W[g];
+          e.stride = pl.n / L;
+          e.nunits = e.stride;
+          e.gNs = pl.Ns[g];
+        }
+      }
+    }
+    st = upload((void**)&r->d_ea, eas);
+  }
   if (st == GFFT_OK) st = upload((void**)&r->d_lane_off, lane_off);
   if (st == GFFT_OK) st = upload((void**)&r->d_offset, offs);
   r->done_bytes = (size_t)count * GFFT_MAXG * sizeof(int);
@@ -408,6 +438,7 @@ static int ragged_launch(gfft_ragged* r, const void* src, void* dst, cudaStream_
   a.tab = r->d_tab;
   a.plans = r->d_plans;
   a.items = r->d_items;
+  a.ea = r->d_ea;
   a.lane_off = r->d_lane_off;
   a.offset = r->d_offset;
   a.done = r->d_done;

@@ -161,6 +161,7 @@ struct RaggedArgs {
   const void* tab;
   const RaggedPlan* plans;
   const RaggedItem* items;
+  const EngineArgs* ea;       // per (plan, global pass): the engine arguments but the buffers
   const long long* lane_off;  // single-pass groups
   const long long* offset;    // element offset of every transform
   int* done;                  // completed tiles per (transform, pass)
