@@ -393,34 +393,39 @@ def _smooth_pool(limit, lo=256):
 def run_planner(args):
     """C5: the cost model trained on autotuner-timed plans (FP32), then plans
     chosen for held-out sizes up to one 2^27 transform; regret against the
-    exhaustive measured search, the default plan's regret beside it."""
+    exhaustive measured search for the model's first choice and for the best
+    measured of its top 3 / top 5 (the pruned search), the default plan's
+    regret beside them.  Training and held-out lengths are drawn from the same
+    5-smooth range [256, 2^27], disjoint; every length runs max(1, 2^20 / n)
+    transforms."""
     import numpy as np
 
     import gfft_gb300
     from gfft_gb300 import tuner
     gfft_gb300.build()
     rng = np.random.default_rng(0x5EED0005)
-    train_pool = _smooth_pool(1 << 22)
-    test_pool = [n for n in _smooth_pool(1 << 27, 1024)]
-    # log-uniform choice over each pool
-    def pick(pool, k):
-        logs = np.log2(np.array(pool, dtype=np.float64))
+    pool = _smooth_pool(1 << 27, 256)
+
+    def pick(cands, k):  # log-uniform over the pool
+        logs = np.log2(np.array(cands, dtype=np.float64))
         target = rng.uniform(logs.min(), logs.max(), size=4 * k)
-        idx = np.unique(np.searchsorted(logs, target).clip(0, len(pool) - 1))
+        idx = np.unique(np.searchsorted(logs, target).clip(0, len(cands) - 1))
         rng.shuffle(idx)
-        return [pool[i] for i in idx[:k]]
-    train_sizes = pick(train_pool, args.planner_train)
-    test_sizes = [n for n in pick(test_pool, args.planner_test) if n not in set(train_sizes)]
+        return [cands[i] for i in idx[:k]]
+    test_sizes = pick([n for n in pool if n >= 1024], args.planner_test)
     if (1 << 27) not in test_sizes:
         test_sizes[-1:] = [1 << 27]
+    held = set(test_sizes)
+    train_sizes = pick([n for n in pool if n not in held], args.planner_train)
     t0 = time.perf_counter()
-    rows = tuner.timing_table(train_sizes, vtype=1, batch_points=1 << 21, reps=3)
+    rows = tuner.timing_table(train_sizes, vtype=1, batch_points=1 << 20, reps=3)
     t_collect = time.perf_counter() - t0
     X = np.array([r["features"] for r in rows], dtype=np.float32)
     ms = np.array([r["ms"] for r in rows], dtype=np.float32)
+    groups = np.array([r["n"] for r in rows])
     model = tuner.CostModel(seed=7)
     t0 = time.perf_counter()
-    loss = model.fit(X, ms, epochs=4000, lr=3e-3)
+    loss = model.fit(X, ms, epochs=4000, lr=3e-3, groups=groups)
     t_train = time.perf_counter() - t0
     res = []
     for n in test_sizes:
@@ -430,30 +435,30 @@ def run_planner(args):
         ok = t > 0
         best = float(np.min(t[ok]))
         Xc = np.stack([tuner.features(n, 1, 0, 1, b, c) for c in cands])
-        pred = model.predict_ms(Xc)
-        pred = np.where(ok, pred, np.inf)
+        pred = np.where(ok, model.predict_ms(Xc), np.inf)
         order = np.argsort(pred)
-        top1 = float(t[order[0]])
-        top3 = float(np.min(t[order[:3]][t[order[:3]] > 0]))
+        top = {k: float(np.min(np.where(t[order[:k]] > 0, t[order[:k]], np.inf))) for k in (1, 3, 5)}
         dflt = float(t[cands.index({})])
-        res.append({"n": n, "batch": b, "candidates": len(cands), "best_ms": best, "model_ms": top1,
-                    "pruned3_ms": top3, "default_ms": dflt, "best_gflops": tuner.gflops(n, b, best),
-                    "model_gflops": tuner.gflops(n, b, top1)})
-    reg = np.array([r["model_ms"] / r["best_ms"] - 1 for r in res])
-    reg3 = np.array([r["pruned3_ms"] / r["best_ms"] - 1 for r in res])
-    regd = np.array([r["default_ms"] / r["best_ms"] - 1 for r in res])
+        res.append({"n": n, "batch": b, "candidates": len(cands), "best_ms": best, "model_ms": top[1],
+                    "pruned3_ms": top[3], "pruned5_ms": top[5], "default_ms": dflt,
+                    "best_gflops": tuner.gflops(n, b, best), "model_gflops": tuner.gflops(n, b, top[1])})
+
+    def stats(key):
+        r = np.array([x[key] / x["best_ms"] - 1 for x in res])
+        return {"mean": float(r.mean()), "median": float(np.median(r)), "p90": float(np.quantile(r, 0.9)),
+                "within_5pct": float(np.mean(r <= 0.05))}
     big = [r for r in res if r["n"] == 1 << 27]
-    line = {"config": "c5 learned planner, FP32, %d training sizes (%d timed plans), %d held-out sizes <= 2^27"
-                      % (len(train_sizes), len(rows), len(res)),
-            "train_rows": len(rows), "collect_s": t_collect, "train_s": t_train, "train_mse_log_ms": loss,
-            "regret_model_mean": float(reg.mean()), "regret_model_median": float(np.median(reg)),
-            "regret_model_p90": float(np.quantile(reg, 0.9)), "within_5pct_model": float(np.mean(reg <= 0.05)),
-            "regret_pruned3_mean": float(reg3.mean()), "within_5pct_pruned3": float(np.mean(reg3 <= 0.05)),
-            "regret_default_mean": float(regd.mean()), "within_5pct_default": float(np.mean(regd <= 0.05)),
-            "model_gflops_total": float(sum(5.0 * r["n"] * math.log2(r["n"]) * r["batch"] for r in res)
-                                        / sum(r["model_ms"] for r in res) / 1e6),
-            "best_gflops_total": float(sum(5.0 * r["n"] * math.log2(r["n"]) * r["batch"] for r in res)
-                                       / sum(r["best_ms"] for r in res) / 1e6),
+    fl = sum(5.0 * r["n"] * math.log2(r["n"]) * r["batch"] for r in res)
+    line = {"config": "c5 learned planner, FP32, %d training lengths (%d timed plans), %d held-out lengths "
+                      "in [1024, 2^27]" % (len(train_sizes), len(rows), len(res)),
+            "train_rows": len(rows), "collect_s": t_collect, "train_s": t_train, "train_mse_rel_log_ms": loss,
+            "regret_model_top1": stats("model_ms"), "regret_pruned_top3": stats("pruned3_ms"),
+            "regret_pruned_top5": stats("pruned5_ms"), "regret_default": stats("default_ms"),
+            "mean_candidates": float(np.mean([r["candidates"] for r in res])),
+            "gflops_total_model_top1": fl / sum(r["model_ms"] for r in res) / 1e6,
+            "gflops_total_pruned_top5": fl / sum(r["pruned5_ms"] for r in res) / 1e6,
+            "gflops_total_default": fl / sum(r["default_ms"] for r in res) / 1e6,
+            "gflops_total_best": fl / sum(r["best_ms"] for r in res) / 1e6,
             "n_2pow27": big[0] if big else None}
     print(json.dumps(line), flush=True)
     if args.planner_out:

@@ -80,8 +80,19 @@ __device__ __forceinline__ void twiddle_sweep(const EngineArgs& a, typename Vec<
 
 }  // namespace lane
 
+// launch bounds (threads, resident blocks per SM) the registers are sized
+// for: FP32 launches 512-thread blocks and fits 64 registers (two blocks,
+// 32 warps per SM); FP64 launches 256-thread blocks (planner.cpp)
+template <typename T> struct LaneCfg;
+template <> struct LaneCfg<float> {
+  static constexpr int NT = 512, MINB = 2;
+};
+template <> struct LaneCfg<double> {
+  static constexpr int NT = 512, MINB = 1;
+};
+
 template <typename T>
-__global__ void __launch_bounds__(512) lane_kernel(const __grid_constant__ EngineArgs a) {
+__global__ void __launch_bounds__(LaneCfg<T>::NT, LaneCfg<T>::MINB) lane_kernel(const __grid_constant__ EngineArgs a) {
   using namespace lane;
   typedef typename Vec<T>::t V;
   extern __shared__ __align__(16) unsigned char smem_raw[];

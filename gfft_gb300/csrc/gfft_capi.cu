@@ -228,6 +228,13 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)
                                          : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
+      if (gp.variant == 6 && !(opts && opts->blocks_per_sm)) {
+        // two blocks fit by registers (launch bound) and shared memory whenever
+        // two footprints plus the per-block reservation fit one SM
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device);
+        if (2 * (gp.smem + 1024) <= (size_t)smem_sm) per = std::max(per, 2);
+      }
       if (per < 1) per = 1;
       long long grid = (long long)nsm * per;
       if (grid > gp.ntiles) grid = gp.ntiles;

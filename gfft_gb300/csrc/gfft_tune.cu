@@ -154,27 +154,26 @@ int gfft_plan_features(uint64_t n, int vtype_id, int trans_id, int place_id, uin
   f[0] = (float)std::log2((double)n);
   for (int i = 0; i < 4; ++i) f[1 + i] = (float)e[i];
   f[5] = (float)std::log2((double)batch);
-  f[6] = (float)std::log2((double)n / (double)info.pass_len[0]);  // lane stride of the first pass
-  f[7] = (float)dbl;
-  f[8] = (float)info.n_global_passes;
+  f[6] = (float)dbl;
+  f[7] = (float)info.n_global_passes;
   const int rlist[7] = {16, 8, 4, 2, 3, 5, 7};
-  for (int g = 0; g < info.n_global_passes; ++g)
-    for (int i = 0; i < 16 && info.radices[g][i]; ++i) {
-      bool known = false;
+  double lw = 0.0;
+  int lmax = 0, lmin = 1 << 30;
+  for (int g = 0; g < info.n_global_passes; ++g) {
+    for (int i = 0; i < 16 && info.radices[g][i]; ++i)
       for (int k = 0; k < 7; ++k)
-        if (info.radices[g][i] == rlist[k]) {
-          f[9 + k] += 1.0f;
-          known = true;
-        }
-      if (!known) f[16] += 1.0f;
-    }
-  f[17] = (float)std::log2((double)info.threads[0] / (double)std::max(1, info.units[0]));
-  f[18] = (float)info.kernel_variant[0];
-  f[19] = opts ? (float)opts->stages : 0.0f;
-  f[20] = (float)std::log2((double)std::max(1, info.units[0]));
-  f[21] = opts ? (float)opts->radix_order : 0.0f;
-  f[22] = (float)std::log2((double)n * (double)batch * (dbl ? 16.0 : 8.0));
-  f[23] = (opts && opts->max_pass_len) ? (float)std::log2((double)opts->max_pass_len) : 0.0f;
+        if (info.radices[g][i] == rlist[k]) f[8 + k] += 1.0f;
+    lw += std::log2((double)std::max(1, info.units[g]));
+    lmax = std::max(lmax, info.pass_len[g]);
+    lmin = std::min(lmin, info.pass_len[g]);
+    const int v = info.kernel_variant[g];
+    f[v <= 1 ? 18 : (v <= 3 ? 19 : (v == 4 ? 20 : 21))] += 1.0f;
+  }
+  f[15] = (float)(lw / std::max(1, info.n_global_passes));  // mean log2 units (transforms or lanes per block)
+  f[16] = (float)std::log2((double)std::max(1, lmax));
+  f[17] = (float)std::log2((double)std::max(1, lmin));
+  f[22] = opts ? (float)opts->stages : 0.0f;
+  f[23] = (float)info.radices[0][0] / 16.0f;  // the first radix (radix order)
   return GFFT_OK;
 }
 

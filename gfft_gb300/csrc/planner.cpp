@@ -285,7 +285,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       if (3 * W * padded(gp.L) * esz <= 200 * 1024) {
         gp.variant = 4;
         gp.units = (int)W;
-        gp.threads = 256;
+        gp.threads = dbl ? 256 : 512;  // fft_lane.cu LaneCfg
         gp.ntiles = (batch * stride + W - 1) / W;
         gp.smem = (size_t)(3 * W * padded(gp.L) * esz);  // prefetch buffer + ping-pong pair
       }

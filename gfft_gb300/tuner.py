@@ -123,18 +123,35 @@ class MLP:
 
 class CostModel:
     """log(ms) of a plan from its features; inputs standardised with the
-    training set's mean and spread."""
+    training set's mean and spread.
+
+    With ``groups`` (one key per row, e.g. the transform length) the target is
+    the log-time relative to the mean over the rows of the same group: plans
+    are only ever compared within one (length, batch), so the network spends
+    its capacity on the differences between plans rather than on the overall
+    scale, and predictions rank the candidates of a length directly."""
 
     def __init__(self, seed=1):
         self.net = MLP(seed=seed)
         self.mu = np.zeros(_lib.NFEAT, dtype=np.float32)
         self.sd = np.ones(_lib.NFEAT, dtype=np.float32)
 
-    def fit(self, X, ms, epochs=3000, lr=3e-3):
+    @staticmethod
+    def relative_log(ms, groups):
+        y = np.log(np.asarray(ms, dtype=np.float64))
+        g = np.asarray(groups)
+        out = np.empty_like(y)
+        for key in np.unique(g):
+            sel = g == key
+            out[sel] = y[sel] - y[sel].mean()
+        return out.astype(np.float32)
+
+    def fit(self, X, ms, epochs=3000, lr=3e-3, groups=None):
         X = np.asarray(X, dtype=np.float32)
         self.mu = X.mean(0)
         self.sd = np.where(X.std(0) > 1e-6, X.std(0), 1.0).astype(np.float32)
-        return self.net.train((X - self.mu) / self.sd, np.log(np.asarray(ms, dtype=np.float32)), epochs, lr)
+        y = self.relative_log(ms, groups) if groups is not None else np.log(np.asarray(ms, dtype=np.float32))
+        return self.net.train((X - self.mu) / self.sd, y, epochs, lr)
 
     def predict_ms(self, X):
         X = (np.asarray(X, dtype=np.float32) - self.mu) / self.sd

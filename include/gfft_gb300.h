@@ -158,10 +158,12 @@ int gfft_tune_measure(uint64_t n, int vtype_id, int trans_id, int place_id, uint
                       const gfft_plan_opts* cands, int ncands, const void* d_src, void* d_dst, int reps,
                       float* ms_out);
 /* Feature vector (GFFT_NFEAT floats) of the plan these options give:
- * log2 N, exponents of 2/3/5/7, log2 batch, log2 lane stride of the first
- * pass, dtype, global passes, counts of radices 16/8/4/2/3/5/7 and of generic
- * primes, log2 threads per transform, kernel variant, stages, log2 units,
- * radix order, log2 bytes, log2 pass-length cap.  No GPU needed. */
+ * [0] log2 N, [1-4] exponents of 2/3/5/7, [5] log2 batch, [6] FP64, [7]
+ * global passes, [8-14] counts of in-block radices 16/8/4/2/3/5/7, [15] mean
+ * log2 units per block, [16] log2 longest and [17] shortest pass length,
+ * [18-21] passes run by the generic engine / the pipelined single-pass
+ * kernels / the prefetching column tiles / the specialised column tiles,
+ * [22] pipeline stages requested, [23] first radix / 16.  No GPU needed. */
 int gfft_plan_features(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
                        const gfft_plan_opts* opts, float* features);
 

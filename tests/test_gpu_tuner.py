@@ -48,7 +48,7 @@ def test_learned_planner_regret(cuda):
     X = np.array([r["features"] for r in rows], dtype=np.float32)
     ms = np.array([r["ms"] for r in rows], dtype=np.float32)
     model = tuner.CostModel(seed=11)
-    loss = model.fit(X, ms, epochs=2500)
+    loss = model.fit(X, ms, epochs=2500, groups=[r["n"] for r in rows])
     assert loss < 0.5
     regrets, base = [], []
     for n in test_sizes:

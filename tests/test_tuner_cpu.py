@@ -25,10 +25,20 @@ def test_features():
     assert f.shape == (_lib.NFEAT,)
     assert abs(f[0] - np.log2(2 ** 10 * 3 ** 5)) < 1e-5
     assert list(f[1:5]) == [10, 5, 0, 0]
-    assert f[5] == 3 and f[7] == 0 and f[8] == 2
-    assert f[9:16].sum() >= 4  # radices counted
+    assert f[5] == 3 and f[6] == 0 and f[7] == 2
+    assert f[8:15].sum() >= 4  # radices counted
+    assert f[18:22].sum() == 2  # one kernel class per global pass
+    assert abs(f[16] - np.log2(576)) < 1e-5 and abs(f[17] - np.log2(432)) < 1e-5
     g = tuner.features(4096, 0, 0, 1, 1, {"max_radix": 4})
-    assert g[7] == 1 and g[11] == 6  # six radix-4 passes, FP64
+    assert g[6] == 1 and g[10] == 6  # six radix-4 passes, FP64
+    assert g[23] == 4 / 16
+    # candidates that differ only in their pipeline depth or lane width differ in features
+    h1 = tuner.features(4096, 1, 0, 1, 64, {"stages": 3})
+    h0 = tuner.features(4096, 1, 0, 1, 64, {})
+    assert h1[22] == 3 and h0[22] == 0
+    w0 = tuner.features(1 << 20, 1, 0, 1, 1, {"kernel_variant": 4})
+    w1 = tuner.features(1 << 20, 1, 0, 1, 1, {"units_per_block": 16})
+    assert w1[15] > w0[15]
 
 
 def test_mlp_reference_gradients_finite_difference():
