@@ -179,6 +179,72 @@ template <typename T, typename V> __device__ __forceinline__ void dft16(V* v) {
   for (int i = 0; i < 16; ++i) v[i] = o[i];
 }
 
+template <typename T, typename V, int R> __device__ __forceinline__ void dft(V* v);
+
+// Composite radix R = A * B with gcd(A, B) = 1 (6, 10, 12, 15): the
+// prime-factor (Good-Thomas) split needs no twiddles.  Input n = (n1 B + n2 A)
+// mod R, output k = (k1 B (B^-1 mod A) + k2 A (A^-1 mod B)) mod R; then
+// W_R^{nk} = W_A^{n1 k1} W_B^{n2 k2}: B transforms of length A, A of length B.
+constexpr int inv_mod(int x, int m) {
+  int r = 1;
+  while ((x * r) % m != 1) ++r;
+  return r;
+}
+template <typename T, typename V, int A, int B> __device__ __forceinline__ void dft_pfa(V* v) {
+  constexpr int R = A * B;
+  constexpr int BI = inv_mod(B % A, A), AI = inv_mod(A % B, B);
+  V t[R];
+#pragma unroll
+  for (int n2 = 0; n2 < B; ++n2) {
+    V y[A];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) y[n1] = v[(n1 * B + n2 * A) % R];
+    dft<T, V, A>(y);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) t[k1 * B + n2] = y[k1];
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) {
+    V z[B];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) z[n2] = t[k1 * B + n2];
+    dft<T, V, B>(z);
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) v[(k1 * B * BI + k2 * A * AI) % R] = z[k2];
+  }
+}
+
+// radix 9 = 3 x 3 (Cooley-Tukey): X[k1 + 3 k2] = sum_n2 W_3^{n2 k2} W_9^{n2 k1}
+// sum_n1 x[3 n1 + n2] W_3^{n1 k1}
+template <typename T, typename V> __device__ __forceinline__ void dft9(V* v) {
+  // W_9^m = cos(2 pi m / 9) - i sin(2 pi m / 9), m = 1, 2, 4
+  const V w1 = mk<V>((T)0.766044443118978035202392650555416674, (T)-0.642787609686539326322643409907263433);
+  const V w2 = mk<V>((T)0.173648177666930348851716626769314796, (T)-0.984807753012208059366743024589523014);
+  const V w4 = mk<V>((T)-0.93969262078590838405410927732473147, (T)-0.342020143325668733044099614682259581);
+  V t[9];
+#pragma unroll
+  for (int n2 = 0; n2 < 3; ++n2) {
+    V y[3] = {v[n2], v[3 + n2], v[6 + n2]};
+    dft3<T, V>(y);
+    t[n2] = y[0];
+    t[3 + n2] = y[1];
+    t[6 + n2] = y[2];
+  }
+  // twiddles W_9^{n2 k1} on t[3 k1 + n2]
+  t[4] = cmul(t[4], w1);
+  t[5] = cmul(t[5], w2);
+  t[7] = cmul(t[7], w2);
+  t[8] = cmul(t[8], w4);
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1) {
+    V z[3] = {t[3 * k1], t[3 * k1 + 1], t[3 * k1 + 2]};
+    dft3<T, V>(z);
+    v[k1] = z[0];
+    v[k1 + 3] = z[1];
+    v[k1 + 6] = z[2];
+  }
+}
+
 template <typename T, typename V, int R> __device__ __forceinline__ void dft(V* v) {
   if constexpr (R == 2) dft2(v[0], v[1]);
   else if constexpr (R == 3) dft3<T, V>(v);
@@ -187,6 +253,11 @@ template <typename T, typename V, int R> __device__ __forceinline__ void dft(V* 
   else if constexpr (R == 7) dft_odd<T, V, 7>(v);
   else if constexpr (R == 8) dft8<T, V>(v);
   else if constexpr (R == 16) dft16<T, V>(v);
+  else if constexpr (R == 6) dft_pfa<T, V, 2, 3>(v);
+  else if constexpr (R == 10) dft_pfa<T, V, 2, 5>(v);
+  else if constexpr (R == 12) dft_pfa<T, V, 4, 3>(v);
+  else if constexpr (R == 15) dft_pfa<T, V, 3, 5>(v);
+  else if constexpr (R == 9) dft9<T, V>(v);
 }
 
 }  // namespace gfft

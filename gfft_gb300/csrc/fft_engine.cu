@@ -39,6 +39,11 @@ __global__ void __launch_bounds__(512) engine_kernel(const __grid_constant__ Eng
       case 3: block_pass<T, 3>(src, dst, a, bp, tw); break;
       case 5: block_pass<T, 5>(src, dst, a, bp, tw); break;
       case 7: block_pass<T, 7>(src, dst, a, bp, tw); break;
+      case 6: block_pass<T, 6>(src, dst, a, bp, tw); break;
+      case 9: block_pass<T, 9>(src, dst, a, bp, tw); break;
+      case 10: block_pass<T, 10>(src, dst, a, bp, tw); break;
+      case 12: block_pass<T, 12>(src, dst, a, bp, tw); break;
+      case 15: block_pass<T, 15>(src, dst, a, bp, tw); break;
       default: block_pass_generic<T>(src, dst, a, bp, tw); break;
     }
     __syncthreads();

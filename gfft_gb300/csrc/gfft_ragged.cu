@@ -118,6 +118,11 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
         case 3: block_pass<T, 3>(src, dst, ea, bp, tw); break;
         case 5: block_pass<T, 5>(src, dst, ea, bp, tw); break;
         case 7: block_pass<T, 7>(src, dst, ea, bp, tw); break;
+        case 6: block_pass<T, 6>(src, dst, ea, bp, tw); break;
+        case 9: block_pass<T, 9>(src, dst, ea, bp, tw); break;
+        case 10: block_pass<T, 10>(src, dst, ea, bp, tw); break;
+        case 12: block_pass<T, 12>(src, dst, ea, bp, tw); break;
+        case 15: block_pass<T, 15>(src, dst, ea, bp, tw); break;
         default: block_pass_generic<T>(src, dst, ea, bp, tw); break;
       }
       __syncthreads();

@@ -15,8 +15,11 @@
 //    with exact integer angle reduction and rounded once to the working type,
 //    so there is no recurrence error.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <map>
 #include <vector>
 
 #include "plan.h"
@@ -96,6 +99,49 @@ bool spec_radices(const GlobalPass& gp) {
   return ok;
 }
 
+// radices with a register butterfly (butterflies.cuh); any other prime runs
+// the generic O(R^2) pass with its own root table
+bool native_radix(int R) {
+  switch (R) {
+    case 2: case 3: case 4: case 5: case 6: case 7: case 8: case 9: case 10: case 12: case 15: case 16: return true;
+    default: return false;
+  }
+}
+
+// The fewest in-block passes for L = 2^a 3^b 5^c 7^d out of the register
+// butterflies {16, 15, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2}; among equally short
+// sequences the one with the larger radices first (descending comparison).
+// Returned largest first.
+std::vector<int> group_radices(int a, int b, int c, int d) {
+  static const int R[12] = {16, 15, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+  static const int E[12][4] = {{4, 0, 0, 0}, {0, 1, 1, 0}, {2, 1, 0, 0}, {1, 0, 1, 0}, {0, 2, 0, 0}, {3, 0, 0, 0},
+                               {0, 0, 0, 1}, {1, 1, 0, 0}, {0, 0, 1, 0}, {2, 0, 0, 0}, {0, 1, 0, 0}, {1, 0, 0, 0}};
+  std::map<std::array<int, 4>, std::vector<int>> memo;
+  std::function<std::vector<int>(std::array<int, 4>)> best = [&](std::array<int, 4> e) -> std::vector<int> {
+    if (e[0] == 0 && e[1] == 0 && e[2] == 0 && e[3] == 0) return {};
+    auto it = memo.find(e);
+    if (it != memo.end()) return it->second;
+    std::vector<int> out;
+    bool have = false;
+    for (int i = 0; i < 12; ++i) {
+      std::array<int, 4> r = e;
+      bool ok = true;
+      for (int k = 0; k < 4; ++k) ok = ok && (r[k] -= E[i][k]) >= 0;
+      if (!ok) continue;
+      std::vector<int> cand = best(r);
+      cand.push_back(R[i]);
+      std::sort(cand.rbegin(), cand.rend());
+      if (!have || cand.size() < out.size() || (cand.size() == out.size() && cand > out)) {
+        out = cand;
+        have = true;
+      }
+    }
+    memo[e] = out;
+    return out;
+  };
+  return best({a, b, c, d});
+}
+
 std::vector<int> block_radices(int L, const PlanOpts& o) {
   std::vector<int> pow2, odd, gen;
   int a = 0;
@@ -103,6 +149,31 @@ std::vector<int> block_radices(int L, const PlanOpts& o) {
   while (m % 2 == 0) {
     m /= 2;
     ++a;
+  }
+  if (m > 1 && o.max_radix >= 16) {
+    // mixed radix with the default radix cap: composite butterflies
+    int e[3] = {0, 0, 0};
+    const int pr[3] = {3, 5, 7};
+    int rest = m;
+    for (int i = 0; i < 3; ++i)
+      while (rest % pr[i] == 0) {
+        rest /= pr[i];
+        ++e[i];
+      }
+    std::vector<int> seq = group_radices(a, e[0], e[1], e[2]);
+    for (const PF& f : factorize(rest))
+      for (int i = 0; i < f.k; ++i) gen.push_back((int)f.p);
+    if (o.radix_order == 2) {  // odd radices (and generic primes) first
+      std::vector<int> oddf, evenf;
+      for (int r : seq) (r % 2 ? oddf : evenf).push_back(r);
+      seq = gen;
+      seq.insert(seq.end(), oddf.begin(), oddf.end());
+      seq.insert(seq.end(), evenf.begin(), evenf.end());
+    } else {
+      seq.insert(seq.end(), gen.begin(), gen.end());
+      if (o.radix_order == 1) std::reverse(seq.begin(), seq.end());
+    }
+    return seq;
   }
   int mr = o.max_radix;
   int lg = mr >= 16 ? 4 : mr >= 8 ? 3 : mr >= 4 ? 2 : 1;
@@ -221,8 +292,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     }
     for (int i = 0; i < gp.npass; ++i) {
       BlockPass& bp = gp.pass[i];
-      if (bp.R > 16 || (bp.R != 2 && bp.R != 3 && bp.R != 4 && bp.R != 5 && bp.R != 7 && bp.R != 8 &&
-                        bp.R != 16)) {
+      if (!native_radix(bp.R)) {
         bp.gen = (int)tw;
         tw += bp.R;
       }
