@@ -95,7 +95,7 @@ int parse_opts(const gfft_plan_opts* opts, PlanOpts& po) {
 
 int check_ids(uint64_t n, int vtype_id, int trans_id, int dim, int parall_id, int place_id, uint64_t batch) {
   if (vtype_id < 0 || vtype_id > 3) return GFFT_E_INVALID_TYPE;
-  if (trans_id < 0 || trans_id > 3) return GFFT_E_INVALID_TRANSFORM;
+  if (trans_id < 0 || trans_id > 7) return GFFT_E_INVALID_TRANSFORM;
   if (place_id < 0 || place_id > 1) return GFFT_E_INVALID_PLACE;
   if (dim != 1) return GFFT_E_INVALID_DIM;
   if (parall_id < 0) return GFFT_E_INVALID_PARALL;
@@ -159,6 +159,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
   *handle = nullptr;
   int st0 = check_ids(n, vtype_id, trans_id, dim, parall_id, place_id, batch);
   if (st0 != GFFT_OK) return st0;
+  if (trans_id >= 4) return gfft_dct_create(handle, n, vtype_id, trans_id, parall_id, place_id, batch);
   PlanOpts po;
   st0 = parse_opts(opts, po);
   if (st0 != GFFT_OK) return st0;
@@ -263,6 +264,9 @@ int gfft_create(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int
 int gfft_destroy(gfft_handle h) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   h->magic = 0;
+  if (h->dct_inner) gfft_destroy(h->dct_inner);
+  for (int i = 0; i < 2; ++i)
+    if (h->d_dct[i]) cudaFree(h->d_dct[i]);
   cudaFree(h->d_tab);
   for (int i = 0; i < 2; ++i)
     if (h->d_ws[i]) cudaFree(h->d_ws[i]);
@@ -285,6 +289,16 @@ int gfft_destroy(gfft_handle h) {
 int gfft_get_info(gfft_handle h, gfft_plan_info* info) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   if (!info) return GFFT_E_NULL_POINTER;
+  if (h->dct_inner) {  // the inner real transform's plan, under this handle's identity
+    int st = gfft_get_info(h->dct_inner, info);
+    if (st != GFFT_OK) return st;
+    info->n = (uint64_t)h->hp.n;
+    info->trans_id = h->trans_id;
+    info->place_id = h->place_id;
+    info->workspace_bytes += 2 * (uint64_t)h->dct_bytes;
+    info->kernels_per_exec += 2;
+    return GFFT_OK;
+  }
   fill_info(h->hp, h->vtype, h->tab_bytes, h->ws_bytes, info);
   return GFFT_OK;
 }
@@ -299,6 +313,18 @@ int gfft_plan_query(uint64_t n, int vtype_id, int trans_id, int place_id, uint64
   if (st != GFFT_OK) return st;
   HostPlan hp;
   const int dbl = (vtype_id == 0 || vtype_id == 2) ? 1 : 0;
+  if (trans_id >= 4) {  // cosine transform: the inner real transform's plan
+    if (vtype_id > 1) return GFFT_E_INVALID_TYPE;
+    const bool one = trans_id <= 5;
+    if (one && n < 2) return GFFT_E_INVALID_SIZE;
+    st = gfft_plan_query(one ? n - 1 : n, vtype_id, 2, 1, batch, opts, info);
+    if (st != GFFT_OK) return st;
+    info->n = n;
+    info->trans_id = trans_id;
+    info->place_id = place_id;
+    info->kernels_per_exec += 2;
+    return GFFT_OK;
+  }
   if (gfft_plan_build(hp, (long long)n, (long long)batch, dbl, trans_id, place_id, po) != 0)
     return GFFT_E_INVALID_SIZE;
   const size_t esz = elem_bytes(dbl);
@@ -441,6 +467,7 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
 int gfft_get_device_status(gfft_handle h, int* status) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   if (!status) return GFFT_E_NULL_POINTER;
+  if (h->dct_inner) return gfft_get_device_status(h->dct_inner, status);
   if (cudaDeviceSynchronize() != cudaSuccess) return GFFT_E_CUDA;
   if (cudaMemcpy(status, h->d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return GFFT_E_CUDA;
   if (cudaMemset(h->d_status, 0, sizeof(int)) != cudaSuccess) return GFFT_E_CUDA;
@@ -503,6 +530,7 @@ int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
   const size_t al = h->hp.dbl ? 16 : 8;
   if (((uintptr_t)src % al) || ((uintptr_t)dst % al)) return GFFT_E_MISALIGNED;
   if (h->hp.place == 0 && src != dst) return GFFT_E_INVALID_PLACE;
+  if (h->dct_inner) return gfft_dct_exec(h, src, dst, (cudaStream_t)stream);
   return gfft_exec_ws(h, src, dst, (cudaStream_t)stream, h->d_ws[0], h->d_ws[1]);
 }
 
@@ -587,7 +615,9 @@ int gfft_exec_host(gfft_handle h, const void* src, void* dst, gfft_stream stream
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   if (!src || !dst) return GFFT_E_NULL_POINTER;
   if (h->hp.place == 0 && src != dst) return GFFT_E_INVALID_PLACE;
-  const size_t bytes = (size_t)h->hp.n * (size_t)h->hp.batch * elem_bytes(h->hp.dbl);
+  // complex elements, or reals for a cosine transform
+  const size_t bytes =
+      (size_t)h->hp.n * (size_t)h->hp.batch * elem_bytes(h->hp.dbl) / (h->dct_inner ? 2 : 1);
   if (!h->d_stage) {
     if (cudaMalloc(&h->d_stage, bytes) != cudaSuccess) {
       h->d_stage = nullptr;
@@ -596,9 +626,10 @@ int gfft_exec_host(gfft_handle h, const void* src, void* dst, gfft_stream stream
     h->stage_bytes = bytes;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  if (bytes >= (64ull << 20) && h->hp.batch >= 4) return exec_host_chunked(h, src, dst, s);
+  if (bytes >= (64ull << 20) && h->hp.batch >= 4 && !h->dct_inner) return exec_host_chunked(h, src, dst, s);
   if (cudaMemcpyAsync(h->d_stage, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return GFFT_E_CUDA;
-  int st = gfft_exec_ws(h, h->d_stage, h->d_stage, s, h->d_ws[0], h->d_ws[1]);
+  int st = h->dct_inner ? gfft_dct_exec(h, h->d_stage, h->d_stage, s)
+                        : gfft_exec_ws(h, h->d_stage, h->d_stage, s, h->d_ws[0], h->d_ws[1]);
   if (st != GFFT_OK) return st;
   if (cudaMemcpyAsync(dst, h->d_stage, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return GFFT_E_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return GFFT_E_CUDA;

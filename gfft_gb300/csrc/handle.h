@@ -36,7 +36,19 @@ struct gfft_plan {
   cudaEvent_t ev_in[GFFT_MAX_CHUNKS] = {};
   cudaEvent_t ev_done[GFFT_MAX_CHUNKS] = {};
   cudaEvent_t ev_user = nullptr, ev_end = nullptr;
+  // cosine transforms (transform IDs 4-7): pre pass, this inner real
+  // transform of length dct_m (complex half-length), post pass
+  gfft_plan* dct_inner = nullptr;
+  int dct_type = 0;  // 1 or 2, 0 for every other transform
+  long long dct_m = 0;
+  void* d_dct[2] = {nullptr, nullptr};  // the extended input and the packed spectrum
+  size_t dct_bytes = 0;
 };
+
+// cosine transforms (defined in gfft_dct.cu)
+extern "C" int gfft_dct_create(gfft_plan** handle, uint64_t n, int vtype_id, int trans_id, int parall_id,
+                               int place_id, uint64_t batch);
+extern "C" int gfft_dct_exec(gfft_plan* h, const void* src, void* dst, cudaStream_t stream);
 
 // Runs a plan with the given workspace buffers (defined in gfft_capi.cu).
 extern "C" int gfft_exec_ws(gfft_plan* h, const void* src, void* dst, cudaStream_t stream, void* ws0, void* ws1);

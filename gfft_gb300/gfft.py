@@ -86,7 +86,33 @@ class IRDFT(_Tag):
     Sign = -1
 
 
+class DCT1(_Tag):
+    """X_k = sum_l x_l cos(pi k l / (n-1)) (the reference's direct.h DCT1)."""
+    ID = 4
+    Sign = 1
+
+
+class IDCT1(_Tag):
+    """The DCT1 sum divided by n (the reference's Backward policy)."""
+    ID = 5
+    Sign = -1
+
+
+class DCT2(_Tag):
+    """X_k = sum_l x_l cos(pi k l / n) (the reference's direct.h DCT2)."""
+    ID = 6
+    Sign = 1
+
+
+class IDCT2(_Tag):
+    """The DCT2 sum divided by n."""
+    ID = 7
+    Sign = -1
+
+
 DFT.Inverse, IDFT.Inverse, RDFT.Inverse, IRDFT.Inverse = IDFT, DFT, IRDFT, RDFT
+DCT1.Inverse, IDCT1.Inverse, DCT2.Inverse, IDCT2.Inverse = IDCT1, DCT1, IDCT2, DCT2
+COSINE_TYPES = (DCT1, IDCT1, DCT2, IDCT2)
 
 
 class IN_PLACE(_Tag):
@@ -115,7 +141,7 @@ def OpenMP(NT: int):
 
 
 VALUE_TYPES = {0: DOUBLE, 1: FLOAT, 2: COMPLEX_DOUBLE, 3: COMPLEX_FLOAT}
-TRANSFORM_TYPES = {0: DFT, 1: IDFT, 2: RDFT, 3: IRDFT}
+TRANSFORM_TYPES = {0: DFT, 1: IDFT, 2: RDFT, 3: IRDFT, 4: DCT1, 5: IDCT1, 6: DCT2, 7: IDCT2}
 PLACES = {0: IN_PLACE, 1: OUT_OF_PLACE}
 
 
@@ -193,7 +219,7 @@ class TransformObject:
     # number of scalars (real dtype) of one batch
     @property
     def scalars(self):
-        return 2 * self.n * self.batch
+        return (1 if self.Type in COSINE_TYPES else 2) * self.n * self.batch
 
     def info(self):
         inf = _lib.PlanInfo()

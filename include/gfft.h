@@ -18,7 +18,7 @@
  *   GenerateTransform / CreateTransformObject   src/gfftgen.h:189-231
  *   TransformFactoryError::Exception            src/gfftgen.h:133-145
  *   AbstractFFT_inp / AbstractFFT_oop           src/gfftpolicy.h:46-58
- *   tags DOUBLE..COMPLEX_FLOAT, DFT..IRDFT,
+ *   tags DOUBLE..COMPLEX_FLOAT, DFT..IRDFT (and DCT1..IDCT2),
  *   IN_PLACE/OUT_OF_PLACE, Serial/OpenMP<NT>    src/gfftpolicy.h:78-453
  *   groups (Default / FullList)                 src/gfftparamgroups.h:30-78
  *   Transform<...>::Instance                    src/gfftgen.h:46-87
@@ -133,6 +133,30 @@ struct IRDFT {
   static const id_t ID = 3;
   static const int Sign = -1;
   typedef RDFT Inverse;
+};
+/* Cosine transforms of n reals (DOUBLE / FLOAT): the sums of the reference's
+ * direct.h (src/direct.h:270-312); the I* tags divide by n (Backward). */
+struct IDCT1;
+struct IDCT2;
+struct DCT1 {
+  static const id_t ID = 4;
+  static const int Sign = 1;
+  typedef IDCT1 Inverse;
+};
+struct IDCT1 {
+  static const id_t ID = 5;
+  static const int Sign = -1;
+  typedef DCT1 Inverse;
+};
+struct DCT2 {
+  static const id_t ID = 6;
+  static const int Sign = 1;
+  typedef IDCT2 Inverse;
+};
+struct IDCT2 {
+  static const id_t ID = 7;
+  static const int Sign = -1;
+  typedef DCT2 Inverse;
 };
 
 struct Serial {
@@ -252,7 +276,7 @@ class ObjectBase : public Base {
   void run_host(const T* src, T* dst) { check(gfft_exec_host(h_.get(), src, dst, nullptr)); }
   detail::Handle& inverse() {
     if (!inv_) {
-      static const int inv_of[4] = {1, 0, 3, 2};
+      static const int inv_of[8] = {1, 0, 3, 2, 5, 4, 7, 6};
       inv_ = new Handle(n_, vt_, inv_of[tr_], par_, pl_, batch_);
     }
     return *inv_;

@@ -19,6 +19,12 @@
  *   - RDFT (trans_id 2) of length n transforms 2n reals into the packed
  *     half spectrum X_0, X_n, X_1 .. X_{n-1}; IRDFT (3) inverts it,
  *     IRDFT(RDFT(x)) = x (src/gfftswap.h:239-287, src/gfftpolicy.h:262-297);
+ *   - DCT1 (4) / DCT2 (6) of n reals (value types DOUBLE / FLOAT) compute the
+ *     reference's direct sums X_k = sum_{l<n} x_l cos(pi k l / (n - 1)) and
+ *     X_k = sum_{l<n} x_l cos(pi k l / n) (src/direct.h:270-312; the
+ *     reference's DCT policies, src/gfftpolicy.h:302-365, have no algorithm);
+ *     IDCT1 (5) / IDCT2 (7) are the same sums under the reference's Backward
+ *     policy, divided by n (src/gfftswap.h:355-361); n >= 2 for types 1;
  *   - value type IDs DOUBLE=0, FLOAT=1, COMPLEX_DOUBLE=2, COMPLEX_FLOAT=3;
  *     place IDs IN_PLACE=0, OUT_OF_PLACE=1; parallel IDs Serial=0,
  *     OpenMP<NT>=NT-1 (src/gfftpolicy.h:78-453).  Every parallel ID maps to
@@ -48,7 +54,7 @@ enum {
   GFFT_OK = 0,
   GFFT_E_INVALID_SIZE = 1,      /* n == 0, batch == 0, or a length this build cannot plan */
   GFFT_E_INVALID_TYPE = 2,      /* vtype_id not in {0,1,2,3} */
-  GFFT_E_INVALID_TRANSFORM = 3, /* trans_id not in {0,1,2,3} */
+  GFFT_E_INVALID_TRANSFORM = 3, /* trans_id not in {0 .. 7} */
   GFFT_E_INVALID_PLACE = 4,     /* place_id not in {0,1}, or in place with src != dst */
   GFFT_E_INVALID_DIM = 5,       /* dim != 1 */
   GFFT_E_INVALID_PARALL = 6,    /* parall_id < 0 */
@@ -67,7 +73,8 @@ enum {
  * trans_id, dim, parall_id, place_id) (src/gfftgen.h:222-231) plus the
  * Transform::Create() it ends in (src/gfftgen.h:81-83).  `n` is the transform
  * length (complex points; for RDFT/IRDFT the complex length of the packed
- * 2n reals).  `batch` transforms lie back to back (stride 2n scalars). */
+ * 2n reals; for the cosine transforms the number of reals).  `batch`
+ * transforms lie back to back (stride 2n scalars, n for a cosine transform). */
 int gfft_create(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim, int parall_id,
                 int place_id, uint64_t batch);
 

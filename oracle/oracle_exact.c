@@ -153,6 +153,29 @@ void orc_rdft_q(int64_t n, const double* in, double* out) {
   }
 }
 
+/* Direct cosine transforms as the reference defines them (src/direct.h:270-312,
+ * structs DCT1 and DCT2), summed in binary128 with the angle reduced exactly:
+ *   type 1: X_k = sum_{l<n} x_l cos(pi k l / (n - 1)),  n >= 2
+ *   type 2: X_k = sum_{l<n} x_l cos(pi k l / n)
+ * (the reference's `inverse` flag only flips the sign of pi, which cos
+ * ignores).  cos(pi m / M) = cos(2 pi m / (2M)), m = k l mod 2M. */
+void orc_dct_q(int64_t n, int type, const double* in, double* out) {
+  const int64_t M = type == 1 ? n - 1 : n;
+  const int64_t P = 2 * M;
+  for (int64_t k = 0; k < n; ++k) {
+    q_t acc = 0;
+    int64_t idx = 0;
+    for (int64_t l = 0; l < n; ++l) {
+      q_t c, sn;
+      q_root(idx, P, &c, &sn);
+      acc += (q_t)in[l] * c;
+      idx += k % P;
+      if (idx >= P) idx -= P;
+    }
+    out[k] = (double)acc;
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* long double mixed-radix FFT with exactly reduced twiddles                */
 

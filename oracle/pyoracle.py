@@ -43,6 +43,7 @@ def lib():
         L.orc_dft_bins_q.argtypes = [i64, dp, i64, vp, dp, ci]
         L.orc_fft_ld.argtypes = [i64, i64, dp, dp, ci]
         L.orc_rdft_q.argtypes = [i64, dp, dp]
+        L.orc_dct_q.argtypes = [i64, ci, dp, dp]
         L.orc_gen_uniform.argtypes = [ctypes.c_uint64, i64, dp]
         L.orc_num_threads.restype = ci
         _lib = L
@@ -117,6 +118,15 @@ def rdft_q(x):
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.zeros_like(x)
     lib().orc_rdft_q(x.size // 2, x.ctypes.data, y.ctypes.data)
+    return y
+
+
+def dct_q(x, dct_type):
+    """Direct cosine transform of the reference's direct.h (type 1 or 2) of
+    the n reals ``x``, binary128 accumulation."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    lib().orc_dct_q(x.size, int(dct_type), x.ctypes.data, y.ctypes.data)
     return y
 
 

@@ -129,3 +129,18 @@ def test_reference_accuracy_large_n(oracle):
     exact = oracle.fft_ld(x, n, 1, 1)
     rel = np.linalg.norm(y - exact) / np.linalg.norm(exact)
     assert rel < 1e-10
+
+
+def test_dct_oracle_against_mpmath(oracle):
+    """The direct cosine sums of the reference's direct.h (DCT1, DCT2),
+    summed in binary128, against 40-digit sums."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(3)
+    for n in (2, 3, 7, 16, 33):
+        x = rng.uniform(-1, 1, n)
+        for t in (1, 2):
+            M = n - 1 if t == 1 else n
+            ref = [float(mp.fsum(mp.mpf(float(x[l])) * mp.cos(mp.pi * k * l / M) for l in range(n)))
+                   for k in range(n)]
+            assert np.max(np.abs(oracle.dct_q(x, t) - np.array(ref))) <= 1e-15 * n, (n, t)
