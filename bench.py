@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--planner-out", default="", help="directory for the timing table and model weights")
     p.add_argument("--opts", default="", help="with --suite: plan options as JSON, e.g. '{\"kernel_variant\": 1}'")
     p.add_argument("--only", default="", help="with --suite: run the configurations whose name contains this")
+    p.add_argument("--ragged-count", type=int, default=10000,
+                   help="with --suite: transforms of the ragged configuration (10000 = C4; fewer for profiling)")
     p.add_argument("--case", action="store_true",
                    help="one FP32 C2C transform of --n x --batch with --opts, --warmup + --steps launches, device "
                         "buffers only (small profiling runs)")
@@ -224,7 +226,7 @@ def run_ragged(args, peak):
 
     from gfft_gb300 import gfft as G
     from gfft_gb300 import inputs
-    sizes = inputs.ragged_sizes(0x5EED0004, 10000, 6, 18)
+    sizes = inputs.ragged_sizes(0x5EED0004, args.ragged_count, 6, 18)
     total = int(sizes.sum())
     x = torch.rand(2 * total, device="cuda", dtype=torch.float32).mul_(2).sub_(1)
     y = torch.empty_like(x)
@@ -243,7 +245,8 @@ def run_ragged(args, peak):
     fl = float(sum(5.0 * n * math.log2(n) for n in sizes if n > 1))
     alg = 16.0 * total
     info = rb.info()
-    line = {"config": "c4 fp32 ragged 10000 lengths 2^6..2^18 (5-smooth), one persistent launch, graph replay",
+    line = {"config": "c4 fp32 ragged %d lengths 2^6..2^18 (5-smooth), one persistent launch, graph replay"
+                      % len(sizes),
             "transforms": len(sizes), "total_points": total, "ms": ms, "GFLOP/s": fl / ms / 1e6,
             "GB/s_algorithmic": alg / ms / 1e6, "frac_hbm": alg / ms / 1e6 / peak, "status": rb.status(), **info}
     print(json.dumps(line), flush=True)
