@@ -21,7 +21,7 @@ STATUS_NAMES = {
 }
 
 # every symbol the header declares, checked by the CPU tests
-EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
+EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_create_nd", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
             "gfft_get_info", "gfft_plan_query", "gfft_get_device_status", "gfft_selftest_bounded_wait",
             "gfft_exec_noalloc", "gfft_ragged_create", "gfft_ragged_exec", "gfft_ragged_get_info",
             "gfft_ragged_get_status", "gfft_ragged_destroy", "gfft_tune_candidates", "gfft_tune_measure",
@@ -74,6 +74,7 @@ def lib():
         vp, ci, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64
         L.gfft_create.argtypes = [ctypes.POINTER(vp), u64, ci, ci, ci, ci, ci, u64]
         L.gfft_create_opts.argtypes = [ctypes.POINTER(vp), u64, ci, ci, ci, ci, ci, u64, ctypes.POINTER(PlanOpts)]
+        L.gfft_create_nd.argtypes = [ctypes.POINTER(vp), ci, ctypes.POINTER(u64), ci, ci, ci, u64]
         L.gfft_exec.argtypes = [vp, vp, vp, vp]
         L.gfft_exec_host.argtypes = [vp, vp, vp, vp]
         L.gfft_destroy.argtypes = [vp]

@@ -188,7 +188,7 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
     const long long t = u / a.stride;
     const long long b = u - t * a.stride;
     const long long k = b % a.gNs;
-    const long long kstep = k * (a.N / (a.gNs * L));  // twiddle exponent per sample
+    const long long kstep = a.notw ? 0 : k * (a.N / (a.gNs * L));  // twiddle exponent per sample
     const int lgB = 63 - __clzll(a.gB);
     const V* src = in + t * a.N + b;
     for (int s0 = threadIdx.x / W; s0 < L; s0 += 8 * sstep) {

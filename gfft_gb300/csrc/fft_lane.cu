@@ -65,7 +65,7 @@ __device__ __forceinline__ void twiddle_sweep(const EngineArgs& a, typename Vec<
   const long long u = tile * W + lane;
   const long long b = u % a.stride;
   const long long k = b % a.gNs;
-  const long long kstep = k * (a.N / (a.gNs * L));
+  const long long kstep = a.notw ? 0 : k * (a.N / (a.gNs * L));
   if (!kstep && !a.conj) return;
   V* bl = buf + lane * a.Lp;
   const int sstep = blockDim.x / W;

@@ -137,7 +137,7 @@ const char* gfft_strerror(int status) {
     case GFFT_E_INVALID_TYPE: return "invalid value type id";
     case GFFT_E_INVALID_TRANSFORM: return "invalid transform type id";
     case GFFT_E_INVALID_PLACE: return "invalid place id (in place requires src == dst)";
-    case GFFT_E_INVALID_DIM: return "only one-dimensional transforms are implemented";
+    case GFFT_E_INVALID_DIM: return "dimension not supported (1, 2 or 3; several dimensions for complex DFT/IDFT only)";
     case GFFT_E_INVALID_PARALL: return "invalid parallelization id";
     case GFFT_E_NULL_POINTER: return "null pointer";
     case GFFT_E_MISALIGNED: return "pointer not aligned to a complex element";
@@ -157,6 +157,10 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                      int place_id, uint64_t batch, const gfft_plan_opts* opts) {
   if (!handle) return GFFT_E_NULL_POINTER;
   *handle = nullptr;
+  if ((dim == 2 || dim == 3) && trans_id <= 1 && parall_id >= 0 && !opts) {  // an n^dim array
+    const uint64_t dims[3] = {n, n, n};
+    return gfft_create_nd(handle, dim, dims, vtype_id, trans_id, place_id, batch);
+  }
   int st0 = check_ids(n, vtype_id, trans_id, dim, parall_id, place_id, batch);
   if (st0 != GFFT_OK) return st0;
   if (trans_id >= 4) return gfft_dct_create(handle, n, vtype_id, trans_id, parall_id, place_id, batch);
@@ -265,6 +269,9 @@ int gfft_destroy(gfft_handle h) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   h->magic = 0;
   if (h->dct_inner) gfft_destroy(h->dct_inner);
+  if (h->nd_inner) gfft_destroy(h->nd_inner);
+  for (int i = 0; i < 2; ++i)
+    if (h->nd_tab[i]) cudaFree(h->nd_tab[i]);
   for (int i = 0; i < 2; ++i)
     if (h->d_dct[i]) cudaFree(h->d_dct[i]);
   cudaFree(h->d_tab);
@@ -289,6 +296,15 @@ int gfft_destroy(gfft_handle h) {
 int gfft_get_info(gfft_handle h, gfft_plan_info* info) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   if (!info) return GFFT_E_NULL_POINTER;
+  if (h->nd_inner) {  // the innermost axis's plan plus one column pass per outer axis
+    int st = gfft_get_info(h->nd_inner, info);
+    if (st != GFFT_OK) return st;
+    info->n = (uint64_t)h->hp.n;
+    info->batch = (uint64_t)h->hp.batch;
+    for (int d = 0; d < h->nd_rank - 1; ++d)
+      if (h->nd_dims[d] > 1) ++info->kernels_per_exec;
+    return GFFT_OK;
+  }
   if (h->dct_inner) {  // the inner real transform's plan, under this handle's identity
     int st = gfft_get_info(h->dct_inner, info);
     if (st != GFFT_OK) return st;
@@ -468,6 +484,7 @@ int gfft_get_device_status(gfft_handle h, int* status) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   if (!status) return GFFT_E_NULL_POINTER;
   if (h->dct_inner) return gfft_get_device_status(h->dct_inner, status);
+  if (h->nd_inner) return gfft_get_device_status(h->nd_inner, status);
   if (cudaDeviceSynchronize() != cudaSuccess) return GFFT_E_CUDA;
   if (cudaMemcpy(status, h->d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return GFFT_E_CUDA;
   if (cudaMemset(h->d_status, 0, sizeof(int)) != cudaSuccess) return GFFT_E_CUDA;
@@ -531,6 +548,7 @@ int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
   if (((uintptr_t)src % al) || ((uintptr_t)dst % al)) return GFFT_E_MISALIGNED;
   if (h->hp.place == 0 && src != dst) return GFFT_E_INVALID_PLACE;
   if (h->dct_inner) return gfft_dct_exec(h, src, dst, (cudaStream_t)stream);
+  if (h->nd_inner) return gfft_nd_exec(h, src, dst, (cudaStream_t)stream);
   return gfft_exec_ws(h, src, dst, (cudaStream_t)stream, h->d_ws[0], h->d_ws[1]);
 }
 
@@ -626,10 +644,12 @@ int gfft_exec_host(gfft_handle h, const void* src, void* dst, gfft_stream stream
     h->stage_bytes = bytes;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  if (bytes >= (64ull << 20) && h->hp.batch >= 4 && !h->dct_inner) return exec_host_chunked(h, src, dst, s);
+  if (bytes >= (64ull << 20) && h->hp.batch >= 4 && !h->dct_inner && !h->nd_inner)
+    return exec_host_chunked(h, src, dst, s);
   if (cudaMemcpyAsync(h->d_stage, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return GFFT_E_CUDA;
-  int st = h->dct_inner ? gfft_dct_exec(h, h->d_stage, h->d_stage, s)
-                        : gfft_exec_ws(h, h->d_stage, h->d_stage, s, h->d_ws[0], h->d_ws[1]);
+  int st = h->dct_inner  ? gfft_dct_exec(h, h->d_stage, h->d_stage, s)
+           : h->nd_inner ? gfft_nd_exec(h, h->d_stage, h->d_stage, s)
+                         : gfft_exec_ws(h, h->d_stage, h->d_stage, s, h->d_ws[0], h->d_ws[1]);
   if (st != GFFT_OK) return st;
   if (cudaMemcpyAsync(dst, h->d_stage, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return GFFT_E_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return GFFT_E_CUDA;

@@ -43,12 +43,24 @@ struct gfft_plan {
   long long dct_m = 0;
   void* d_dct[2] = {nullptr, nullptr};  // the extended input and the packed spectrum
   size_t dct_bytes = 0;
+  // multi-dimensional transforms (gfft_create_nd): the innermost axis as
+  // this inner batched plan, every outer axis as one column pass (no
+  // four-step twiddle) in place on the output
+  gfft_plan* nd_inner = nullptr;
+  int nd_rank = 0;
+  long long nd_dims[3] = {1, 1, 1};
+  GlobalPass nd_gp[2];
+  long long nd_stride[2] = {0, 0};
+  void* nd_tab[2] = {nullptr, nullptr};
+  unsigned nd_grid[2] = {0, 0};
 };
 
 // cosine transforms (defined in gfft_dct.cu)
 extern "C" int gfft_dct_create(gfft_plan** handle, uint64_t n, int vtype_id, int trans_id, int parall_id,
                                int place_id, uint64_t batch);
 extern "C" int gfft_dct_exec(gfft_plan* h, const void* src, void* dst, cudaStream_t stream);
+// multi-dimensional transforms (defined in gfft_nd.cu)
+extern "C" int gfft_nd_exec(gfft_plan* h, const void* src, void* dst, cudaStream_t stream);
 
 // Runs a plan with the given workspace buffers (defined in gfft_capi.cu).
 extern "C" int gfft_exec_ws(gfft_plan* h, const void* src, void* dst, cudaStream_t stream, void* ws0, void* ws1);

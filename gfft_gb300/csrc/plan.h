@@ -98,6 +98,7 @@ struct EngineArgs {
   FastDiv fd_half;    // L/2 + 1 (real pre/post pass)
   const long long* lane_off;  // mode 2: element offset of each lane's transform
   int ldcg;           // read the input through L2 only (data written by other blocks of this launch)
+  int notw;           // lane passes without the four-step twiddle (axis transforms of a multi-dimensional array)
   BlockPass pass[GFFT_MAXP];
 };
 
@@ -197,3 +198,5 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
 // Fill `tab` (2*table_count doubles, interleaved) with every table the plan
 // references, generated in extended precision and rounded once.
 void gfft_plan_tables(const HostPlan& plan, double* tab);
+// true when a power-of-two pass uses the length-specialised kernels' radices
+bool spec_radices(const GlobalPass& gp);

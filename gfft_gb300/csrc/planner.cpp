@@ -24,6 +24,8 @@
 
 #include "plan.h"
 
+bool spec_radices(const GlobalPass& gp);
+
 namespace {
 
 struct PF {
@@ -78,25 +80,6 @@ void wroot(long long j, long long m, double* re, double* im) {
   root(j, m, &c, &s);
   *re = (double)c;
   *im = (double)(-s);
-}
-
-// The in-block radices of the length-specialised kernels for a power-of-two
-// L: radix 16 while four bits remain, the remainder as 8 x 4 (one bit), 4 or
-// 8 (fft_spec.cu, spec.cuh radix_of).
-bool spec_radices(const GlobalPass& gp) {
-  int lg = 0;
-  while ((1LL << lg) < gp.L) ++lg;
-  if ((1LL << lg) != gp.L || lg < 4) return false;
-  std::vector<int> want((std::size_t)(lg / 4), 16);
-  if (lg % 4 == 1) {
-    want.back() = 8;
-    want.push_back(4);
-  } else if (lg % 4) {
-    want.push_back(1 << (lg % 4));
-  }
-  bool ok = (int)want.size() == gp.npass;
-  for (int i = 0; i < gp.npass && ok; ++i) ok = gp.pass[i].R == want[(std::size_t)i];
-  return ok;
 }
 
 // radices with a register butterfly (butterflies.cuh); any other prime runs
@@ -232,6 +215,26 @@ bool split_passes(long long N, int P, long long cap, std::vector<long long>& out
 int round32(long long x) { return (int)std::max<long long>(32, (x + 31) / 32 * 32); }
 
 }  // namespace
+
+// The in-block radices of the length-specialised kernels for a power-of-two
+// L: radix 16 while four bits remain, the remainder as 8 x 4 (one bit), 4 or
+// 8 (fft_spec.cu, spec.cuh radix_of).
+bool spec_radices(const GlobalPass& gp) {
+  int lg = 0;
+  while ((1LL << lg) < gp.L) ++lg;
+  if ((1LL << lg) != gp.L || lg < 4) return false;
+  std::vector<int> want((std::size_t)(lg / 4), 16);
+  if (lg % 4 == 1) {
+    want.back() = 8;
+    want.push_back(4);
+  } else if (lg % 4) {
+    want.push_back(1 << (lg % 4));
+  }
+  bool ok = (int)want.size() == gp.npass;
+  for (int i = 0; i < gp.npass && ok; ++i) ok = gp.pass[i].R == want[(std::size_t)i];
+  return ok;
+}
+
 
 int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int trans, int place,
                     const PlanOpts& opts) {

@@ -174,7 +174,7 @@ __device__ __forceinline__ void sweep(const EngineArgs& a, typename Vec<T>::t* b
   const long long u = tile * W + lane;
   const unsigned b = (unsigned)(u % a.stride);
   const unsigned k = b % (unsigned)a.gNs;
-  const unsigned kstep = k * (unsigned)(a.N / (a.gNs * L));
+  const unsigned kstep = a.notw ? 0u : k * (unsigned)(a.N / (a.gNs * L));
   if (!kstep && !a.conj) return;
   V* bl = buf + lane * LP;
   const V* lo = (const V*)a.gtw_lo;

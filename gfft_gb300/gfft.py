@@ -301,6 +301,37 @@ class TransformObject:
             pass
 
 
+class TransformND(TransformObject):
+    """A multi-dimensional complex DFT / IDFT of ``batch`` row-major arrays of
+    shape ``dims`` (1 to 3 axes, the last fastest) through
+    ``gfft_create_nd``; ``fft`` as for ``TransformObject``.  No reference
+    counterpart (the reference implements only ``Dim = 1``)."""
+
+    def __init__(self, dims, vtype, trans=None, place=None, batch=1):
+        self.dims = tuple(int(d) for d in dims)
+        self.n = int(np.prod(self.dims))
+        self.VType = vtype
+        self.Type = trans or DFT
+        self.Parall = Serial
+        self.Place = place or OUT_OF_PLACE
+        self.batch = int(batch)
+        self.dim = len(self.dims)
+        self._inverse = None
+        self._opts = None
+        L = _lib.lib()
+        arr = (ctypes.c_uint64 * len(self.dims))(*self.dims)
+        h = ctypes.c_void_p()
+        _lib.check(L.gfft_create_nd(ctypes.byref(h), len(self.dims), arr, vtype.ID, self.Type.ID, self.Place.ID,
+                                    self.batch), "gfft_create_nd(%s, %s, %s)" % (self.dims, vtype.name(),
+                                                                                 self.Type.name()))
+        self._h = h
+
+    def inverse_object(self):
+        if self._inverse is None:
+            self._inverse = TransformND(self.dims, self.VType, self.Type.Inverse, self.Place, self.batch)
+        return self._inverse
+
+
 class RaggedBatch:
     """Transforms of many lengths (back to back, in the order of ``sizes``)
     in one persistent launch replayed from a CUDA graph (gfft_ragged_*).

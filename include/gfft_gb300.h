@@ -56,7 +56,7 @@ enum {
   GFFT_E_INVALID_TYPE = 2,      /* vtype_id not in {0,1,2,3} */
   GFFT_E_INVALID_TRANSFORM = 3, /* trans_id not in {0 .. 7} */
   GFFT_E_INVALID_PLACE = 4,     /* place_id not in {0,1}, or in place with src != dst */
-  GFFT_E_INVALID_DIM = 5,       /* dim != 1 */
+  GFFT_E_INVALID_DIM = 5,       /* dim / rank not in 1..3 */
   GFFT_E_INVALID_PARALL = 6,    /* parall_id < 0 */
   GFFT_E_NULL_POINTER = 7,
   GFFT_E_MISALIGNED = 8,        /* pointer not aligned to one complex element */
@@ -99,6 +99,17 @@ typedef struct gfft_plan_opts {
 
 int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim,
                      int parall_id, int place_id, uint64_t batch, const gfft_plan_opts* opts);
+
+/* Multi-dimensional complex DFT / IDFT of `batch` row-major arrays of
+ * dims[0] x ... x dims[rank-1] complex points (rank 1..3, the last index
+ * fastest).  No reference counterpart: the reference carries a `Dim`
+ * parameter (src/gfftgen.h:49, 153-154, 200) but implements only Dim = 1.
+ * gfft_create with dim = 2 or 3 builds the n^dim case through this call.
+ * Every axis but the last must be at most 4096 (FP32) / 2048 (FP64) points;
+ * the last any supported 1-D length.  Execute with gfft_exec /
+ * gfft_exec_host; the inverse divides by the product of the dims. */
+int gfft_create_nd(gfft_handle* handle, int rank, const uint64_t* dims, int vtype_id, int trans_id, int place_id,
+                   uint64_t batch);
 
 /* Replaces AbstractFFT_inp<T>::fft(T*) and AbstractFFT_oop<T>::fft(const T*,
  * T*) (src/gfftpolicy.h:46-58) for DEVICE pointers: in place when
