@@ -20,17 +20,30 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
                                            typename Vec<T>::t* __restrict__ dst, const EngineArgs& a,
                                            const BlockPass& p, const typename Vec<T>::t* __restrict__ tw) {
   typedef typename Vec<T>::t V;
+  constexpr int PS = PadShift<T>::v;
   const int L = a.L;
   const int nb = L / R;
   const int total = a.W * nb;
+  // when nb (resp. Ns) is a multiple of the padding period, pad(x + r nb) =
+  // pad(x) + r (nb + nb / 2^PS): the legs sit at a constant padded stride
+  const bool rd_lin = (nb & ((1 << PS) - 1)) == 0;
+  const bool wr_lin = (p.Ns & ((1 << PS) - 1)) == 0;
+  const int rd_st = nb + (nb >> PS);
+  const int wr_st = (int)p.Ns + ((int)p.Ns >> PS);
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
     const int lane = (int)fdiv((unsigned)i, p.fd_nb);
     const int j = i - lane * nb;
     const V* s = src + lane * a.Lp;
     V* d = dst + lane * a.Lp;
     V v[R];
+    if (rd_lin) {
+      const V* s0 = s + pad<T>(j);
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = s[pad<T>(j + r * nb)];
+      for (int r = 0; r < R; ++r) v[r] = s0[r * rd_st];
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = s[pad<T>(j + r * nb)];
+    }
     const int k = j - (int)fdiv((unsigned)j, p.fd_ns) * p.Ns;
     if (p.Ns > 1) {
       const V* t = tw + p.tw + k;
@@ -39,8 +52,14 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
     }
     dft<T, V, R>(v);
     const int base = (j - k) * R + k;
+    if (wr_lin) {
+      V* d0 = d + pad<T>(base);
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[pad<T>(base + r * p.Ns)] = v[r];
+      for (int r = 0; r < R; ++r) d0[r * wr_st] = v[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) d[pad<T>(base + r * p.Ns)] = v[r];
+    }
   }
 }
 
