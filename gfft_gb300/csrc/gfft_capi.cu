@@ -37,6 +37,10 @@ extern "C" int gfft_lanep2_setup(int dbl, size_t max_smem);
 extern "C" int gfft_lanep2_occupancy(int dbl, int L, int threads, size_t smem);
 extern "C" int gfft_lanep2_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                   cudaStream_t stream);
+extern "C" int gfft_mixed_setup(int dbl, size_t max_smem);
+extern "C" int gfft_mixed_occupancy(int dbl, const EngineArgs* a, int threads, size_t smem);
+extern "C" int gfft_mixed_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                 cudaStream_t stream);
 extern "C" int gfft_tc_setup(size_t max_smem);
 extern "C" int gfft_tc_occupancy(int L, int threads, size_t smem);
 extern "C" int gfft_tc_launch(const EngineArgs* a, unsigned grid, unsigned threads, size_t smem, cudaStream_t stream);
@@ -65,11 +69,23 @@ int setup_device_once(int dbl) {
   if (gfft_lane_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_lanep2_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (!dbl && gfft_tc_setup((size_t)maxopt) != 0) return GFFT_E_CUDA;
+  if (gfft_mixed_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (dev < 64) done[dbl][dev] = true;
   return GFFT_OK;
 }
 
 size_t elem_bytes(int dbl) { return dbl ? 16 : 8; }
+
+// occupancy of the compile-time mixed-radix kernel of a pass (selected by
+// its length and radices)
+int mixed_occupancy(int dbl, const GlobalPass& gp) {
+  EngineArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.L = gp.L;
+  a.npass = gp.npass;
+  for (int i = 0; i < gp.npass; ++i) a.pass[i] = gp.pass[i];
+  return gfft_mixed_occupancy(dbl, &a, gp.threads, gp.smem);
+}
 
 int parse_opts(const gfft_plan_opts* opts, PlanOpts& po) {
   if (!opts) return GFFT_OK;
@@ -232,6 +248,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                        : gp.variant == 4 ? gfft_lane_occupancy(dbl, gp.threads, gp.smem)
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)
+                       : gp.variant == 7 ? mixed_occupancy(dbl, gp)
                                          : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
       if (gp.variant == 6 && !(opts && opts->blocks_per_sm)) {
         // two blocks fit by registers (launch bound) and shared memory whenever
@@ -449,6 +466,11 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
       a.ntiles = gp.ntiles;
       a.spin_limit = 1LL << 26;
       if (gfft_tc_launch(&a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      continue;
+    }
+    if (gp.variant == 7) {
+      a.ntiles = gp.ntiles;
+      if (gfft_mixed_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
       continue;
     }
     if (gp.variant == 4 || gp.variant == 5) {

@@ -22,6 +22,7 @@
 #include <map>
 #include <vector>
 
+#include "mixed_shapes.h"
 #include "plan.h"
 
 bool spec_radices(const GlobalPass& gp);
@@ -378,6 +379,24 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.threads = (int)(TILE / 16);
         gp.ntiles = (batch * (n / gp.L)) / W;
         gp.smem = (size_t)(2 * W * padded(gp.L) * esz);  // current tile + the next one's gather
+      }
+    }
+    // compile-time mixed-radix column tiles (fft_mixed.cu) for the shapes of
+    // mixed_shapes.h: passes of a multi-pass length, or single-pass complex
+    // lengths (stride 1); every lane finds its own transform and column, so
+    // a tile may span transforms
+    if ((o.variant == 0 || o.variant == 7) && o.threads == 0 && o.units == 0 && gp.variant != 5 &&
+        gp.variant != 3 && gp.variant != 2 && (gp.mode == 1 || trans < 2) && n < (1LL << 31)) {
+      int rs[GFFT_MAXP];
+      for (int i = 0; i < gp.npass; ++i) rs[i] = gp.pass[i].R;
+      const long long W = mixed_lanes(gp.L, dbl);
+      const long long stride = n / gp.L;
+      if (gp.npass <= 4 && mixed_shape_index(gp.L, rs, gp.npass) >= 0) {
+        gp.variant = 7;
+        gp.units = (int)W;
+        gp.threads = 256;
+        gp.ntiles = (batch * stride + W - 1) / W;
+        gp.smem = (size_t)(3 * W * padded(gp.L) * esz);  // two gathered tiles and the work buffer
       }
     }
     // split-precision tensor-core form, on request: FP32 complex, power-of-two

@@ -81,7 +81,7 @@ def test_plan_column_kernel_selection():
         d = _lib.plan_query(n, vt, 0, 1, 1)
         assert d["n_global_passes"] >= 2 and set(d["kernel_variant"]) == {5}, (n, vt, d)
         assert all(64 <= L <= 1024 for L in d["pass_len"])
-    assert set(_lib.plan_query(5 ** 8, 1, 0, 1, 1)["kernel_variant"]) == {4}
+    assert set(_lib.plan_query(5 ** 8 * 3, 1, 0, 1, 1)["kernel_variant"]) <= {4, 7}
     assert set(_lib.plan_query(1 << 20, 1, 0, 1, 1, {"kernel_variant": 4})["kernel_variant"]) == {4}
     assert set(_lib.plan_query(1 << 20, 1, 0, 1, 1, {"max_radix": 8})["kernel_variant"]) == {4}
     # an 8192-point FP64 transform of two 64 x 128 passes: tile (2048) divides n
@@ -90,6 +90,15 @@ def test_plan_column_kernel_selection():
     # 1024 points in two passes: a 2048-value tile would span transforms
     d = _lib.plan_query(1024, 0, 0, 1, 4, {"max_pass_len": 64})
     assert 5 not in d["kernel_variant"], d
+
+
+def test_plan_mixed_kernel_selection():
+    """Mixed-radix pass shapes with a compile-time kernel take variant 7."""
+    assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8)["kernel_variant"] == [5, 7]
+    assert _lib.plan_query(5 ** 8, 0, 0, 1, 8)["kernel_variant"] == [7, 7]
+    assert _lib.plan_query(768, 1, 0, 1, 100)["kernel_variant"] == [7]
+    assert _lib.plan_query(768, 1, 0, 1, 100, {"kernel_variant": 1})["kernel_variant"] == [1]
+    assert 7 not in _lib.plan_query(768, 1, 2, 1, 100)["kernel_variant"]  # real: fused pre/post in the engine
 
 
 def test_plan_errors():

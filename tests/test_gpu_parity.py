@@ -442,6 +442,31 @@ def test_cpp_facade_on_gpu(cuda):
     assert "facade ok (gpu)" in r.stdout
 
 
+@pytest.mark.parametrize("dbl", [0, 1])
+@pytest.mark.parametrize("n,B", [(768, 7), (625, 5), (576, 3), (432, 9), (1000, 3), (729, 2), (480, 5), (360, 11),
+                                 (3 * 2 ** 18, 2), (5 ** 8, 2), (2 ** 10 * 3 ** 5, 3), (1000 * 1000, 1)])
+def test_mixed_columns(cuda, oracle, n, B, dbl):
+    """The compile-time mixed-radix column tiles (variant 7): single-pass
+    lengths (batches whose last tile is partial) and the passes of multi-pass
+    lengths, forward and inverse, out of place and in place, against the
+    generic engine and the exact oracle."""
+    from gfft_gb300 import _lib
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    assert 7 in _lib.plan_query(n, vt, 0, 1, B)["kernel_variant"]
+    x = inputs.gaussian(23 + n, 2 * n * B).astype(dt)
+    for tr in (0, 1):
+        y = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+        gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
+        assert rel(y, gen) <= tol(n, dbl), (n, tr, rel(y, gen))
+        yi = run_gpu(cuda, n, vt, tr, 0, x, batch=B)
+        assert np.array_equal(y, yi), (n, tr)
+    k = min(B, max(1, (1 << 20) // n))
+    ex = oracle.fft_ld(x[:2 * n * k].astype(np.float64), n, k, 1)
+    y = run_gpu(cuda, n, vt, 0, 1, x[:2 * n * k], batch=k)
+    assert rel(y, ex) <= tol(n, dbl), (n, rel(y, ex))
+
+
 @pytest.mark.parametrize("n,dbl,B,cap", [(1 << 13, 0, 3, 1024), (1 << 16, 0, 2, 0), (1 << 20, 0, 1, 0),
                                          (1 << 24, 0, 1, 0), (1 << 18, 0, 2, 64), (1 << 12, 1, 5, 64),
                                          (1 << 18, 1, 2, 0), (1 << 22, 1, 1, 0), (1 << 15, 0, 3, 256)])
