@@ -12,7 +12,13 @@ template <typename T> struct PadShift;
 template <> struct PadShift<float> { static constexpr int v = 4; };   // 8-byte elements
 template <> struct PadShift<double> { static constexpr int v = 3; };  // 16-byte elements
 
-template <typename T> __device__ __forceinline__ int pad(int s) { return s + (s >> PadShift<T>::v); }
+// padded index: one slot per 2^PS values, and one more per 2^(PS+4) so that
+// strides of 2^(PS+4) values (a multiple of the 128-byte bank window after
+// the first term) fall on different banks; engine_padded (plan.h) is the
+// matching per-unit stride
+template <typename T> __device__ __forceinline__ int pad(int s) {
+  return s + (s >> PadShift<T>::v) + (s >> (PadShift<T>::v + 4));
+}
 
 // one in-block Stockham pass of compile-time radix R over all W units
 template <typename T, int R>
@@ -24,12 +30,13 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
   const int L = a.L;
   const int nb = L / R;
   const int total = a.W * nb;
-  // when nb (resp. Ns) is a multiple of the padding period, pad(x + r nb) =
-  // pad(x) + r (nb + nb / 2^PS): the legs sit at a constant padded stride
-  const bool rd_lin = (nb & ((1 << PS) - 1)) == 0;
-  const bool wr_lin = (p.Ns & ((1 << PS) - 1)) == 0;
-  const int rd_st = nb + (nb >> PS);
-  const int wr_st = (int)p.Ns + ((int)p.Ns >> PS);
+  // when nb (resp. Ns) is a multiple of the longer padding period 2^(PS+4),
+  // pad(x + r nb) = pad(x) + r pad'(nb) with pad'(nb) = nb + nb / 2^PS +
+  // nb / 2^(PS+4): the legs sit at a constant padded stride
+  const bool rd_lin = (nb & ((1 << (PS + 4)) - 1)) == 0;
+  const bool wr_lin = (p.Ns & ((1 << (PS + 4)) - 1)) == 0;
+  const int rd_st = nb + (nb >> PS) + (nb >> (PS + 4));
+  const int wr_st = (int)p.Ns + ((int)p.Ns >> PS) + ((int)p.Ns >> (PS + 4));
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
     const int lane = (int)fdiv((unsigned)i, p.fd_nb);
     const int j = i - lane * nb;

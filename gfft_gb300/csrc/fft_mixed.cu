@@ -29,12 +29,18 @@ template <> struct Cfg<double> {
   static constexpr int TILE = 2048, PS = 3;
 };
 constexpr int lanes(int L, int tile) { return (2 * L <= tile) ? 2 * lanes(2 * L, tile) : 1; }
-template <typename T> __device__ __forceinline__ constexpr int padi(int s) { return s + (s >> Cfg<T>::PS); }
+// padded index: one slot per 2^PS values and one more per 2^(PS+4), so that
+// strides of 2^(PS+4) values (which the first term alone turns into a
+// multiple of the 128-byte bank window) land on different banks
+template <typename T> __device__ __forceinline__ constexpr int padi(int s) {
+  return s + (s >> Cfg<T>::PS) + (s >> (Cfg<T>::PS + 4));
+}
+template <typename T> constexpr int padded_len(int L) { return L + (L >> Cfg<T>::PS) + (L >> (Cfg<T>::PS + 4)) + 1; }
 
 template <typename T, int L, int W>
 __device__ __forceinline__ void gather(const EngineArgs& a, typename Vec<T>::t* buf, long long tile) {
   typedef typename Vec<T>::t V;
-  constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
+  constexpr int LP = padded_len<T>(L);
   const int lane = threadIdx.x % W;
   const long long u = tile * W + lane;
   if (u >= a.nunits) return;
@@ -49,7 +55,7 @@ __device__ __forceinline__ void gather(const EngineArgs& a, typename Vec<T>::t* 
 template <typename T, int L, int W>
 __device__ __forceinline__ void sweep(const EngineArgs& a, typename Vec<T>::t* buf, long long tile) {
   typedef typename Vec<T>::t V;
-  constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
+  constexpr int LP = padded_len<T>(L);
   const int lane = threadIdx.x % W;
   const long long u = tile * W + lane;
   const unsigned b = (unsigned)(u % a.stride);
@@ -78,7 +84,7 @@ __device__ __forceinline__ void pass(const typename Vec<T>::t* __restrict__ src,
                                      const typename Vec<T>::t* __restrict__ tw, int twoff) {
   typedef typename Vec<T>::t V;
   constexpr int NB = L / R, TOT = W * NB;
-  constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
+  constexpr int LP = padded_len<T>(L);
   for (int i = threadIdx.x; i < TOT; i += NT) {
     const int lane = i / NB, j = i % NB, k = j % NS;
     const V* s = src + lane * LP;
@@ -107,7 +113,7 @@ __global__ void __launch_bounds__(mixed::NT, 2) mixed_kernel(const __grid_consta
   typedef typename Vec<T>::t V;
   constexpr int L = R0 * R1 * R2 * R3;
   constexpr int W = lanes(L, Cfg<T>::TILE);
-  constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
+  constexpr int LP = padded_len<T>(L);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* const bufs0 = reinterpret_cast<V*>(smem_raw);  // gathered tiles (current / next)
   V* const bufs1 = bufs0 + W * LP;

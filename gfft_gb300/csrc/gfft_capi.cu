@@ -442,7 +442,10 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     a.tw = tab;
     a.rtw = tab + p.rtw_off * esz;
     a.pad_shift = dbl ? 3 : 4;
-    a.Lp = gp.L + (gp.L >> a.pad_shift) + 1;
+    // the run-time engine kernels (variants 1, 4) pad with engine_padded; the
+    // others keep one slot per 2^pad_shift values
+    a.Lp = (gp.variant == 1 || gp.variant == 4) ? (int)engine_padded(gp.L, dbl)
+                                                : gp.L + (gp.L >> a.pad_shift) + 1;
     a.W = gp.units;
     a.mode = gp.mode;
     a.npass = gp.npass;

@@ -60,7 +60,7 @@ int build_axis(gfft_plan* h, int k, long long L, long long s, long long total, i
     gp.variant = 4;
     gp.units = (int)W;
     gp.threads = dbl ? 256 : 512;
-    gp.smem = (size_t)(3 * W * padded(L, dbl) * esz);
+    gp.smem = (size_t)(3 * W * engine_padded(L, dbl) * esz);
   }
   const long long nunits = total / L;
   gp.ntiles = (nunits + gp.units - 1) / gp.units;
@@ -181,7 +181,7 @@ int gfft_nd_exec(gfft_plan* h, const void* src, void* dst, cudaStream_t stream) 
     a.gtw_lo = h->nd_tab[d];
     a.gtw_hi = h->nd_tab[d];
     a.pad_shift = dbl ? 3 : 4;
-    a.Lp = (int)(L + (L >> a.pad_shift) + 1);
+    a.Lp = gp.variant == 4 ? (int)engine_padded(L, dbl) : (int)(L + (L >> a.pad_shift) + 1);
     a.W = gp.units;
     a.mode = 1;
     a.npass = gp.npass;

@@ -137,7 +137,7 @@ bool plan(HostPlan& hp, long long n, long long batch, int dbl, int trans, int pl
   hp.place = place;
   const long long esz = dbl ? 16 : 8;
   const int ps = dbl ? 3 : 4;
-  auto padded = [&](long long L) { return L + (L >> ps) + 1; };
+  auto padded = [&](long long L) { return engine_padded(L, dbl); };  // the engine kernel's stride
   const long long budget = 160 * 1024;
   const long long cap1 = dbl ? 4096 : 8192;
   const int lane_w = dbl ? 4 : 8;

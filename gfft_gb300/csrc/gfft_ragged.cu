@@ -258,7 +258,7 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
       if (hp.nglobal == 1) {
         // groups of whole transforms: about 4096 (FP32) / 2048 (FP64) points
         int W = std::max<int>(1, (r->dbl ? 2048 : 4096) / gp.L);
-        while (W > 1 && 2LL * W * (gp.L + (gp.L >> ps) + 1) * esz > po.smem_budget) --W;
+        while (W > 1 && 2LL * W * engine_padded(gp.L, r->dbl) * esz > po.smem_budget) --W;
         rp.W[g] = W;
       } else {
         // columns per item: a power of two, about TILE points, within the transform
@@ -268,7 +268,7 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
         rp.W[g] = (int)W;
         rp.tiles[g] = (int)((stride + W - 1) / W);
       }
-      lanes_max = std::max<int>(lanes_max, rp.W[g] * (gp.L + (gp.L >> ps) + 1));
+      lanes_max = std::max<int>(lanes_max, (int)(rp.W[g] * engine_padded(gp.L, r->dbl)));
     }
     rp.tab = (long long)(tab.size() / 2);
     rp.gtw_lo = (long long)hp.gtw_lo_off;
@@ -348,7 +348,7 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
         const int L = pl.L[g];
         e.L = L;
         e.pad_shift = ps;
-        e.Lp = L + (L >> ps) + 1;
+        e.Lp = (int)engine_padded(L, r->dbl);
         e.N = pl.n;
         e.npass = pl.npass[g];
         for (int i = 0; i < e.npass; ++i) {

@@ -198,5 +198,12 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
 // Fill `tab` (2*table_count doubles, interleaved) with every table the plan
 // references, generated in extended precision and rounded once.
 void gfft_plan_tables(const HostPlan& plan, double* tab);
+// padded per-unit stride of the run-time engine's shared buffers (variants 1
+// and 4, ragged batches): one slot per 2^ps values and one more per
+// 2^(ps+4) (engine.cuh pad), ps = 4 for 8-byte and 3 for 16-byte elements
+inline long long engine_padded(long long L, int dbl) {
+  const int ps = dbl ? 3 : 4;
+  return L + (L >> ps) + (L >> (ps + 4)) + 1;
+}
 // true when a power-of-two pass uses the length-specialised kernels' radices
 bool spec_radices(const GlobalPass& gp);

@@ -252,7 +252,8 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   const int esz = dbl ? 16 : 8;
   const int pad_shift = dbl ? 3 : 4;
   const long long smem_budget = o.smem_budget > 0 ? o.smem_budget : 160 * 1024;
-  auto padded = [&](long long L) { return L + (L >> pad_shift) + 1; };
+  auto padded = [&](long long L) { return L + (L >> pad_shift) + 1; };  // spec / fast kernels
+  auto epadded = [&](long long L) { return engine_padded(L, dbl); };     // run-time engine kernels
   // largest single-pass length: two padded buffers of one transform
   long long cap1 = dbl ? 4096 : 8192;
   if (o.max_pass_len > 0) cap1 = std::min<long long>(cap1, o.max_pass_len);
@@ -260,7 +261,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   int lane_w = o.units > 0 ? o.units : (dbl ? 4 : 8);  // 64-byte rows
   if (lane_w > 32) lane_w = 32;
   long long capL = 1;
-  while (2 * lane_w * padded(capL * 2) * esz <= smem_budget) capL *= 2;
+  while (2 * lane_w * epadded(capL * 2) * esz <= smem_budget) capL *= 2;
   if (o.max_pass_len > 0) capL = std::min<long long>(capL, o.max_pass_len);
 
   std::vector<long long> Ls;
@@ -305,7 +306,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       long long target = dbl ? 2048 : 4096;  // elements per block
       int W = o.units > 0 ? o.units : (int)std::max<long long>(1, target / gp.L);
       W = (int)std::min<long long>(W, batch);
-      while (W > 1 && 2LL * W * padded(gp.L) * esz > smem_budget) --W;
+      while (W > 1 && 2LL * W * epadded(gp.L) * esz > smem_budget) --W;
       gp.units = W;
     } else {
       // lane units: a power of two that divides the block (each thread keeps one lane)
@@ -318,7 +319,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     int thr = o.threads > 0 ? o.threads : round32(std::min<long long>(512, std::max<long long>(64, elems / 16)));
     gp.threads = thr;
     gp.variant = 1;
-    gp.smem = (size_t)(2LL * gp.units * padded(gp.L) * esz);
+    gp.smem = (size_t)(2LL * gp.units * epadded(gp.L) * esz);
     // register-resident TMA-pipelined path: power-of-two single pass whose
     // radices divide 16, 16 values per thread
     bool pow2ok = gp.mode == 0 && trans < 2 && gp.L >= 16 && (gp.L & (gp.L - 1)) == 0 && o.variant != 1;
@@ -352,16 +353,16 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       const long long stride = n / gp.L;
       long long W = 1;
       if (o.units > 0) {  // requested lane width (a power of two), within 3 buffers of 64 KB
-        while (W * 2 <= o.units && W * 2 <= stride && 3 * W * 2 * padded(gp.L) * esz <= 200 * 1024) W *= 2;
+        while (W * 2 <= o.units && W * 2 <= stride && 3 * W * 2 * epadded(gp.L) * esz <= 200 * 1024) W *= 2;
       } else {
         while (W * 2 * gp.L <= TILE && W * 2 <= stride && W * 2 <= 8) W *= 2;
       }
-      if (3 * W * padded(gp.L) * esz <= 200 * 1024) {
+      if (3 * W * epadded(gp.L) * esz <= 200 * 1024) {
         gp.variant = 4;
         gp.units = (int)W;
         gp.threads = dbl ? 256 : 512;  // fft_lane.cu LaneCfg
         gp.ntiles = (batch * stride + W - 1) / W;
-        gp.smem = (size_t)(3 * W * padded(gp.L) * esz);  // prefetch buffer + ping-pong pair
+        gp.smem = (size_t)(3 * W * epadded(gp.L) * esz);  // prefetch buffer + ping-pong pair
       }
     }
     // column tiles with the length-specialised passes: power-of-two L in
@@ -396,7 +397,8 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.units = (int)W;
         gp.threads = 256;
         gp.ntiles = (batch * stride + W - 1) / W;
-        gp.smem = (size_t)(3 * W * padded(gp.L) * esz);  // two gathered tiles and the work buffer
+        // two gathered tiles and the work buffer, padded as fft_mixed.cu padi
+        gp.smem = (size_t)(3 * W * (padded(gp.L) + (gp.L >> (pad_shift + 4))) * esz);
       }
     }
     // split-precision tensor-core form, on request: FP32 complex, power-of-two
