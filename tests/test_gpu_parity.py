@@ -287,7 +287,9 @@ def test_error_codes(cuda):
     assert L.gfft_exec(obj._h, ctypes.c_void_p(p), ctypes.c_void_p(p), None) == 0
     h = ctypes.c_void_p()
     assert L.gfft_create(ctypes.byref(h), 2 * 4099, 1, 0, 1, 0, 1, 1) == 1
-    assert L.gfft_create(ctypes.byref(h), 64, 0, 0, 2, 0, 1, 1) == 5
+    assert L.gfft_create(ctypes.byref(h), 64, 0, 0, 4, 0, 1, 1) == 5  # four dimensions
+    assert L.gfft_create(ctypes.byref(h), 64, 0, 0, 2, 0, 1, 1) == 0  # 64 x 64
+    assert L.gfft_destroy(h) == 0
     cuda.cuda.synchronize()
     # the context is still usable
     y = run_gpu(cuda, 16, 0, 0, 1, inputs.uniform(1, 32))
