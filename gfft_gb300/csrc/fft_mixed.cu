@@ -35,7 +35,11 @@ constexpr int lanes(int L, int tile) { return (2 * L <= tile) ? 2 * lanes(2 * L,
 template <typename T> __device__ __forceinline__ constexpr int padi(int s) {
   return s + (s >> Cfg<T>::PS) + (s >> (Cfg<T>::PS + 4));
 }
-template <typename T> constexpr int padded_len(int L) { return L + (L >> Cfg<T>::PS) + (L >> (Cfg<T>::PS + 4)) + 1; }
+// per-lane stride: odd (in elements), so that the lanes of a tile read at one
+// sample index fall on different banks; equals engine_padded (plan.h)
+template <typename T> constexpr int padded_len(int L) {
+  return (L + (L >> Cfg<T>::PS) + (L >> (Cfg<T>::PS + 4)) + 1) | 1;
+}
 
 template <typename T, int L, int W>
 __device__ __forceinline__ void gather(const EngineArgs& a, typename Vec<T>::t* buf, long long tile) {

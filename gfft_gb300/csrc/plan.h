@@ -201,9 +201,12 @@ void gfft_plan_tables(const HostPlan& plan, double* tab);
 // padded per-unit stride of the run-time engine's shared buffers (variants 1
 // and 4, ragged batches): one slot per 2^ps values and one more per
 // 2^(ps+4) (engine.cuh pad), ps = 4 for 8-byte and 3 for 16-byte elements
+// The stride is odd (in elements) so that the units of a tile, read at one
+// sample index, fall on different banks.
 inline long long engine_padded(long long L, int dbl) {
   const int ps = dbl ? 3 : 4;
-  return L + (L >> ps) + (L >> (ps + 4)) + 1;
+  const long long v = L + (L >> ps) + (L >> (ps + 4)) + 1;
+  return v | 1;
 }
 // true when a power-of-two pass uses the length-specialised kernels' radices
 bool spec_radices(const GlobalPass& gp);

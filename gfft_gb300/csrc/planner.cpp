@@ -397,8 +397,8 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.units = (int)W;
         gp.threads = 256;
         gp.ntiles = (batch * stride + W - 1) / W;
-        // two gathered tiles and the work buffer, padded as fft_mixed.cu padi
-        gp.smem = (size_t)(3 * W * (padded(gp.L) + (gp.L >> (pad_shift + 4))) * esz);
+        // two gathered tiles and the work buffer, padded as fft_mixed.cu padded_len
+        gp.smem = (size_t)(3 * W * epadded(gp.L) * esz);
       }
     }
     // split-precision tensor-core form, on request: FP32 complex, power-of-two
