@@ -136,7 +136,6 @@ bool plan(HostPlan& hp, long long n, long long batch, int dbl, int trans, int pl
   hp.trans = trans;
   hp.place = place;
   const long long esz = dbl ? 16 : 8;
-  const int ps = dbl ? 3 : 4;
   auto padded = [&](long long L) { return engine_padded(L, dbl); };  // the engine kernel's stride
   const long long budget = 160 * 1024;
   const long long cap1 = dbl ? 4096 : 8192;
