@@ -30,9 +30,59 @@
 
 #include "../../include/gfft_gb300.h"
 #include "engine.cuh"
+#include "mixed_shapes.h"
 #include "plan.h"
 
 namespace gfft {
+
+// One pass of compile-time radix R over the item's W lanes (run-time W and
+// padded stride Lp, compile-time butterfly count per lane, strides and
+// twiddle offsets): src -> dst.
+template <typename T, int L, int R, int NS>
+__device__ __forceinline__ void ct_pass(const typename Vec<T>::t* __restrict__ src,
+                                        typename Vec<T>::t* __restrict__ dst, const EngineArgs& a,
+                                        const typename Vec<T>::t* __restrict__ tw, int twoff) {
+  typedef typename Vec<T>::t V;
+  constexpr int NB = L / R;
+  const int total = a.W * NB;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int lane = i / NB, j = i - lane * NB, k = j % NS;
+    const V* s = src + lane * a.Lp;
+    V v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[pad<T>(j + r * NB)];
+    if constexpr (NS > 1) {
+      const V* t = tw + twoff + k;
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(t + (r - 1) * NS));
+    }
+    dft<T, V, R>(v);
+    V* d = dst + lane * a.Lp;
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[pad<T>(base + r * NS)] = v[r];
+  }
+  __syncthreads();
+}
+
+// the in-block passes of one listed shape (mixed_shapes.h); returns the
+// buffer that holds the result.  Not inlined: one function per shape keeps
+// the kernel's own register frame small.
+template <typename T, int R0, int R1, int R2, int R3>
+__device__ __noinline__ typename Vec<T>::t* ct_passes(typename Vec<T>::t* b0, typename Vec<T>::t* b1,
+                                                      const EngineArgs& a) {
+  typedef typename Vec<T>::t V;
+  constexpr int L = R0 * R1 * R2 * R3;
+  const V* tw = (const V*)a.tw;
+  ct_pass<T, L, R0, 1>(b0, b1, a, tw, a.pass[0].tw);
+  if constexpr (R1 == 1) return b1;
+  ct_pass<T, L, R1, R0>(b1, b0, a, tw, a.pass[1].tw);
+  if constexpr (R2 == 1) return b0;
+  ct_pass<T, L, R2, R0 * R1>(b0, b1, a, tw, a.pass[2].tw);
+  if constexpr (R3 == 1) return b1;
+  ct_pass<T, L, R3, R0 * R1 * R2>(b1, b0, a, tw, a.pass[3].tw);
+  return b0;
+}
 
 // resident blocks per SM the register budget is sized for (70 KB of shared
 // memory per block)
@@ -44,7 +94,7 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ EngineArgs ea;
   __shared__ long long item_s, u0_s;
-  __shared__ int abort_s;
+  __shared__ int abort_s, shape_s;
   V* b0 = reinterpret_cast<V*>(smem_raw);
   V* b1 = b0 + ra.lanes_max;
   int key = -1;  // (plan, pass) whose arguments `ea` holds
@@ -82,6 +132,7 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
         }
         __threadfence();
       }
+      shape_s = sizeof(T) == 8 ? -1 : pl.shape[g];
       if (pl.nglobal == 1) {
         ea.in = ra.in;
         ea.out = ra.out;
@@ -108,7 +159,17 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
     V* src = b0;
     V* dst = b1;
     const V* tw = (const V*)ea.tw;
-    for (int p = 0; p < ea.npass; ++p) {
+    const int sh = shape_s;
+    if constexpr (sizeof(T) == 4) {
+      switch (sh) {
+#define GFFT_RAGGED_CASE(i, a, b, c, d) \
+  case i: src = ct_passes<T, a, b, c, d>(b0, b1, ea); break;
+        GFFT_RAGGED_SHAPES(GFFT_RAGGED_CASE)
+#undef GFFT_RAGGED_CASE
+        default: break;
+      }
+    }
+    for (int p = 0; p < ea.npass && !(sizeof(T) == 4 && sh >= 0); ++p) {
       const BlockPass bp = ea.pass[p];
       switch (bp.R) {
         case 16: block_pass<T, 16>(src, dst, ea, bp, tw); break;
@@ -253,6 +314,11 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
       const GlobalPass& gp = hp.gp[g];
       rp.L[g] = gp.L;
       rp.npass[g] = gp.npass;
+      {
+        int rs[GFFT_MAXP];
+        for (int i = 0; i < gp.npass; ++i) rs[i] = gp.pass[i].R;
+        rp.shape[g] = (!r->dbl && gp.npass <= 4) ? ragged_shape_index(rs, gp.npass) : -1;
+      }
       rp.Ns[g] = gp.Ns;
       for (int i = 0; i < gp.npass; ++i) rp.pass[g][i] = gp.pass[i];
       if (hp.nglobal == 1) {

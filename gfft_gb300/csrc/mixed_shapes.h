@@ -38,3 +38,57 @@ inline int mixed_lanes(int L, int dbl) {
   while (2 * W * L <= tile) W *= 2;
   return W;
 }
+
+// Pass shapes of the ragged kernel's compile-time pass functions (FP32): the
+// most frequent (length, radices) of lengths 2^6..2^18 with 5-smooth sizes
+// under the ragged planner; X(index, R0, R1, R2, R3), 1 = unused.
+#define GFFT_RAGGED_SHAPES(X) \
+  X(0, 15, 12, 2, 1) \
+  X(1, 15, 10, 2, 1) \
+  X(2, 15, 15, 2, 1) \
+  X(3, 16, 5, 5, 1) \
+  X(4, 16, 15, 2, 1) \
+  X(5, 12, 9, 3, 1) \
+  X(6, 15, 5, 5, 1) \
+  X(7, 10, 10, 5, 1) \
+  X(8, 16, 10, 2, 1) \
+  X(9, 16, 12, 2, 1) \
+  X(10, 16, 9, 2, 1) \
+  X(11, 16, 15, 1, 1) \
+  X(12, 10, 5, 5, 1) \
+  X(13, 15, 9, 2, 1) \
+  X(14, 16, 9, 3, 1) \
+  X(15, 15, 15, 1, 1) \
+  X(16, 15, 9, 3, 1) \
+  X(17, 15, 10, 4, 1) \
+  X(18, 9, 9, 6, 1) \
+  X(19, 16, 12, 3, 1) \
+  X(20, 9, 9, 3, 1) \
+  X(21, 10, 10, 2, 1) \
+  X(22, 15, 12, 3, 1) \
+  X(23, 16, 10, 4, 1) \
+  X(24, 15, 12, 1, 1) \
+  X(25, 15, 10, 1, 1) \
+  X(26, 9, 9, 2, 1) \
+  X(27, 16, 10, 1, 1) \
+  X(28, 12, 9, 2, 1) \
+  X(29, 16, 9, 1, 1)
+
+// index of the ragged pass shape with radices rs[0..np), or -1
+inline int ragged_shape_index(const int* rs, int np) {
+  static const int R[][4] = {
+#define GFFT_RAGGED_ROW(i, a, b, c, d) {a, b, c, d},
+      GFFT_RAGGED_SHAPES(GFFT_RAGGED_ROW)
+#undef GFFT_RAGGED_ROW
+  };
+  const int ns = (int)(sizeof(R) / sizeof(R[0]));
+  for (int i = 0; i < ns; ++i) {
+    int n = 0;
+    while (n < 4 && R[i][n] > 1) ++n;
+    if (n != np) continue;
+    bool ok = true;
+    for (int p = 0; p < n && ok; ++p) ok = R[i][p] == rs[p];
+    if (ok) return i;
+  }
+  return -1;
+}

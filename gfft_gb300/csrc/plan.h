@@ -137,6 +137,7 @@ struct RaggedPlan {
   long long n;
   int nglobal;
   int tiles[GFFT_MAXG];    // work items of each global pass (two-pass sizes)
+  int shape[GFFT_MAXG];    // compile-time pass function of each global pass (mixed_shapes.h), -1: none
   int L[GFFT_MAXG], W[GFFT_MAXG], npass[GFFT_MAXG];
   long long Ns[GFFT_MAXG];
   long long tab;           // this size's tables, complex elements from the table base
