@@ -96,3 +96,41 @@ def test_ragged_equals_per_length_objects(cuda):
         r = (torch.linalg.vector_norm(y[seg] - want) / torch.linalg.vector_norm(want)).item()
         assert r <= tol(n, 0), (n, r)
         off += n
+
+
+def test_ragged_shape_functions_cover_and_match(cuda, oracle):
+    """Lengths whose passes run the compile-time pass functions (360 x 400,
+    300 x 450, 480 x 324, ...) and lengths that do not, in one launch,
+    against the exact oracle."""
+    from gfft_gb300 import _lib
+    from gfft_gb300 import gfft as G
+    sizes = np.array([360 * 400, 300 * 450, 480 * 324, 375 * 500, 240, 225, 1000, 7 * 11 * 13, 360, 432 * 576])
+    shaped = 0
+    for n in sizes:
+        d = _lib.plan_query(int(n), 1, 0, 1, 1, {"units_per_block": 4, "max_pass_len": 4096, "kernel_variant": 1})
+        shaped += sum(1 for rs in d["radices"] if tuple(rs) in SHAPES)
+    assert shaped >= 8
+    total = int(sizes.sum())
+    x = inputs.uniform(99, 2 * total).astype(np.float32)
+    rb = G.RaggedBatch(sizes, G.FLOAT, G.DFT)
+    import torch
+    xs = torch.from_numpy(x).cuda()
+    ys = torch.empty_like(xs)
+    rb.fft(xs, ys)
+    torch.cuda.synchronize()
+    assert rb.status() == 0
+    y = ys.cpu().numpy()
+    off = 0
+    for n in sizes:
+        n = int(n)
+        seg = slice(2 * off, 2 * (off + n))
+        ex = oracle.fft_ld(x[seg].astype(np.float64), n, 1, 1)
+        err = np.linalg.norm(y[seg] - ex) / np.linalg.norm(ex)
+        assert err <= 6e-7 * np.log2(n), (n, err)
+        off += n
+
+
+SHAPES = {(15, 12, 2), (15, 10, 2), (15, 15, 2), (16, 5, 5), (16, 15, 2), (12, 9, 3), (15, 5, 5), (10, 10, 5),
+          (16, 10, 2), (16, 12, 2), (16, 9, 2), (16, 15), (10, 5, 5), (15, 9, 2), (16, 9, 3), (15, 15), (15, 9, 3),
+          (15, 10, 4), (9, 9, 6), (16, 12, 3), (9, 9, 3), (10, 10, 2), (15, 12, 3), (16, 10, 4), (15, 12), (15, 10),
+          (9, 9, 2), (16, 10), (12, 9, 2), (16, 9)}
