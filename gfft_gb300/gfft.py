@@ -204,7 +204,7 @@ class TransformObject:
         self.dim = int(dim)
         L = _lib.lib()
         h = ctypes.c_void_p()
-        if opts is None:
+        if not opts:  # None or {}: the default plan
             st = L.gfft_create(ctypes.byref(h), self.n, vtype.ID, trans.ID, self.dim, parall.ID, place.ID,
                                self.batch)
         else:

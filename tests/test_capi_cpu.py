@@ -164,3 +164,8 @@ def test_cpp_facade_factory_errors():
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "facade ok (cpu)" in r.stdout
+
+
+def test_empty_options_mean_default_plan():
+    from gfft_gb300 import tuner
+    assert tuner.features(4096, 1, 0, 1, 8, {}).tolist() == tuner.features(4096, 1, 0, 1, 8, None).tolist()
