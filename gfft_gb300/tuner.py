@@ -15,6 +15,7 @@ from __future__ import annotations
 import ctypes
 import json
 import math
+import os
 
 import numpy as np
 
@@ -167,6 +168,15 @@ class CostModel:
         m.net.set_params(d["params"])
         m.mu, m.sd = d["mu"], d["sd"]
         return m
+
+
+MODEL_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "cost_model_gb300.npz")
+
+
+def default_model():
+    """The cost model trained on a GB300 by ``bench.py --planner`` (FP32
+    plans, lengths 256 .. 2^27), shipped with the package; None if absent."""
+    return CostModel.load(MODEL_FILE) if os.path.exists(MODEL_FILE) else None
 
 
 def choose(model, n, vtype=1, trans=0, place=1, batch=1, k=1, reps=5):
