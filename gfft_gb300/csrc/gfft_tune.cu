@@ -57,7 +57,11 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
     int cap, v, mr, ro, st, w;
   };
   std::vector<K> ks;
-  for (int st : {0, 1, 3}) ks.push_back({0, 0, 16, 0, st, 0});
+  // pipeline depths other than the default (one stage FP32, two FP64)
+  const int dflt_st = (vtype_id == 0 || vtype_id == 2) ? 2 : 1;
+  ks.push_back({0, 0, 16, 0, 0, 0});
+  for (int st : {1, 2, 3})
+    if (st != dflt_st) ks.push_back({0, 0, 16, 0, st, 0});
   // wider column tiles (128- and 256-byte rows) with shorter passes
   for (int cap : {0, 512, 256, 128})
     for (int w : {16, 32}) ks.push_back({cap, 0, 16, 0, 0, w});
