@@ -76,3 +76,12 @@ def test_learned_planner_regret(cuda):
     assert m_tr <= m_df + 0.02
     assert m_tr < m_un
     assert float(np.mean(frac)) <= 0.4
+
+
+def test_shipped_cost_model_prunes(cuda):
+    """The cost model shipped with the package loads and drives a pruned
+    search (the best measured of its top 5) to a valid plan."""
+    model = tuner.default_model()
+    assert model is not None
+    opts, ms = tuner.choose(model, 3 * 2 ** 18, 1, 0, 1, 8, k=5)
+    assert ms > 0 and isinstance(opts, dict)
