@@ -15,10 +15,9 @@
 //     tiles of W columns; the tiles of pass g+1 of a transform may start only
 //     when all of its pass-g tiles are done (a per-(transform, pass) counter).
 //
-// Items are ordered longest transform first; a transform's later-pass tiles
-// follow its earlier-pass tiles about 64 MB of listed work later (so that
-// its intermediate is read back from L2), the single-pass groups come last;
-// persistent blocks take items from a global queue head with atomicAdd.  A
+// Items are ordered largest first (the first passes of the long transforms,
+// then the single-pass groups by length, then the later passes), and
+// persistent blocks take them from a global queue head with atomicAdd.  A
 // later-pass item is taken only after every earlier-pass item was taken by a
 // running block, so its wait always ends; the wait is bounded anyway
 // (RaggedArgs::spin_limit, then GFFT_E_TIMEOUT in the status word).
@@ -355,60 +354,25 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
   }
   std::vector<RaggedItem> items;
   std::vector<long long> lane_off;
-  // the tiles of global pass g of transform t (plan dd)
-  auto add_pass = [&](size_t dd, long long t, int g) {
-    const RaggedPlan& rp = plans[dd];
-    const long long stride = rp.n / rp.L[g];
-    for (int k = 0; k < rp.tiles[g]; ++k) {
-      RaggedItem it;
-      it.plan = (int)dd;
-      it.pass = g;
-      it.transform = (int)t;
-      it.unit0 = (long long)k * rp.W[g];
-      it.count = (int)std::min<long long>(rp.W[g], stride - it.unit0);
-      it.group = 0;
-      items.push_back(it);
-    }
-  };
-  // Multi-pass transforms, longest first.  A transform's pass g+1 tiles
-  // follow its pass g tiles once about kWindow bytes of later tiles have
-  // been listed in between: far enough back that those tiles are done when
-  // a block reaches the next pass (the dependency wait rarely waits), near
-  // enough that the intermediate written by pass g is still in L2.  Every
-  // pass's tiles come after all tiles of the pass before it in the same
-  // transform, so a dependency wait always ends.
-  {
-    const long long kWindow = 64LL << 20;
-    struct Pending {
-      size_t dd;
-      long long t;
-      int next;         // the pass to list next
-      long long mark;   // bytes listed when the previous pass was listed
-    };
-    std::vector<Pending> queue;
-    size_t head = 0;
-    long long listed = 0;
-    auto drain = [&](bool all) {
-      while (head < queue.size() && (all || listed - queue[head].mark >= kWindow)) {
-        Pending pd = queue[head++];
-        add_pass(pd.dd, pd.t, pd.next);
-        listed += plans[pd.dd].n * esz;
-        if (pd.next + 1 < plans[pd.dd].nglobal) queue.push_back({pd.dd, pd.t, pd.next + 1, listed});
-      }
-    };
+  auto add_multi = [&](int g) {
     for (size_t dd = distinct.size(); dd-- > 0;) {
       const RaggedPlan& rp = plans[dd];
-      if (rp.nglobal == 1) continue;
-      for (long long t : members[dd]) {
-        add_pass(dd, t, 0);
-        listed += rp.n * esz;
-        queue.push_back({dd, t, 1, listed});
-        drain(false);
-      }
+      if (rp.nglobal <= g || rp.nglobal == 1) continue;
+      const long long stride = rp.n / rp.L[g];
+      for (long long t : members[dd])
+        for (int k = 0; k < rp.tiles[g]; ++k) {
+          RaggedItem it;
+          it.plan = (int)dd;
+          it.pass = g;
+          it.transform = (int)t;
+          it.unit0 = (long long)k * rp.W[g];
+          it.count = (int)std::min<long long>(rp.W[g], stride - it.unit0);
+          it.group = 0;
+          items.push_back(it);
+        }
     }
-    drain(true);
-  }
-  // single-pass lengths: groups of whole transforms, no dependencies
+  };
+  add_multi(0);
   for (size_t dd = distinct.size(); dd-- > 0;) {
     const RaggedPlan& rp = plans[dd];
     if (rp.nglobal != 1) continue;
@@ -425,6 +389,8 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
       items.push_back(it);
     }
   }
+  add_multi(1);
+  add_multi(2);
   r->nitems = (long long)items.size();
   // device buffers
   int st = GFFT_OK;
