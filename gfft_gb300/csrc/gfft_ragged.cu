@@ -98,11 +98,9 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
   V* b0 = reinterpret_cast<V*>(smem_raw);
   V* b1 = b0 + ra.lanes_max;
   int key = -1;  // (plan, pass) whose arguments `ea` holds
+  if (threadIdx.x == 0) item_s = atomicAdd(ra.head, 1);
   while (true) {
-    if (threadIdx.x == 0) {
-      item_s = atomicAdd(ra.head, 1);
-      abort_s = 0;
-    }
+    if (threadIdx.x == 0) abort_s = 0;
     __syncthreads();
     const long long it = item_s;
     if (it >= ra.nitems) return;
@@ -155,6 +153,12 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
     if (abort_s) return;
     const long long u0 = u0_s;
     load_tile<T>(ea, b0, u0);
+    // claim the next item now: the queue's round trip overlaps this item's
+    // passes (the value is used only after them).  A block never holds a
+    // claim on an item listed before the one it works on, so the dependency
+    // waits still always end.
+    long long next_item = 0;
+    if (threadIdx.x == 0) next_item = atomicAdd(ra.head, 1);
     __syncthreads();
     V* src = b0;
     V* dst = b1;
@@ -194,8 +198,11 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
     store_tile<T>(ea, src, u0);
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0 && ea.mode == 1 && item.pass < ra.plans[item.plan].nglobal - 1)
-      atomicAdd(ra.done + (long long)item.transform * GFFT_MAXG + item.pass, 1);
+    if (threadIdx.x == 0) {
+      if (ea.mode == 1 && item.pass < ra.plans[item.plan].nglobal - 1)
+        atomicAdd(ra.done + (long long)item.transform * GFFT_MAXG + item.pass, 1);
+      item_s = next_item;
+    }
   }
 }
 
