@@ -60,10 +60,11 @@ def parse():
     p.add_argument("--planner-out", default="", help="directory for the timing table and model weights")
     p.add_argument("--opts", default="", help="with --suite: plan options as JSON, e.g. '{\"kernel_variant\": 1}'")
     p.add_argument("--only", default="", help="with --suite: run the configurations whose name contains this")
+    p.add_argument("--dtype", default="f32", choices=["f32", "f64"], help="with --case: FP32 or FP64 complex")
     p.add_argument("--ragged-count", type=int, default=10000,
                    help="with --suite: transforms of the ragged configuration (10000 = C4; fewer for profiling)")
     p.add_argument("--case", action="store_true",
-                   help="one FP32 C2C transform of --n x --batch with --opts, --warmup + --steps launches, device "
+                   help="one C2C transform (--dtype) of --n x --batch with --opts, --warmup + --steps launches, device "
                         "buffers only (small profiling runs)")
     p.add_argument("--suite", action="store_true",
                    help="time every configuration of the workload list (one JSON line each) instead of the headline")
@@ -481,9 +482,10 @@ def run_case(args):
     gfft_gb300.build()
     n, batch = args.n, args.batch
     opts = json.loads(args.opts) if args.opts else None
-    x = torch.rand(2 * n * batch, device="cuda", dtype=torch.float32)
+    dbl = args.dtype == "f64"
+    x = torch.rand(2 * n * batch, device="cuda", dtype=torch.float64 if dbl else torch.float32)
     y = torch.empty_like(x)
-    obj = G.TransformObject(n, G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, batch, opts)
+    obj = G.TransformObject(n, G.DOUBLE if dbl else G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, batch, opts)
     for _ in range(args.warmup):
         obj.fft(x, y)
     torch.cuda.synchronize()
@@ -495,7 +497,7 @@ def run_case(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / max(1, args.steps)
     info = obj.info()
-    print(json.dumps({"case": "fp32 c2c", "n": n, "batch": batch, "opts": opts or {}, "ms": ms,
+    print(json.dumps({"case": "%s c2c" % args.dtype, "n": n, "batch": batch, "opts": opts or {}, "ms": ms,
                       "GFLOP/s": flops(n, batch) / ms / 1e6, "variant": info["kernel_variant"],
                       "pass_len": info["pass_len"]}))
 
