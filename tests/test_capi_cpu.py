@@ -169,3 +169,32 @@ def test_cpp_facade_factory_errors():
 def test_empty_options_mean_default_plan():
     from gfft_gb300 import tuner
     assert tuner.features(4096, 1, 0, 1, 8, {}).tolist() == tuner.features(4096, 1, 0, 1, 8, None).tolist()
+
+
+def test_cosine_transform_plans_and_errors():
+    """Cosine transforms (IDs 4-7) plan as the inner real transform of n - 1
+    (type 1) or n (type 2) complex points; complex value types and a type-1
+    length below two are rejected."""
+    d = _lib.plan_query(1000, 0, 4, 1, 3)
+    assert d["trans_id"] == 4 and d["pass_len"] == [999] and d["kernels_per_exec"] == 3
+    assert _lib.plan_query(1000, 1, 6, 0, 1)["pass_len"] == [1000]
+    with pytest.raises(_lib.GfftError):
+        _lib.plan_query(64, 2, 6, 1)
+    with pytest.raises(_lib.GfftError):
+        _lib.plan_query(1, 0, 4, 1)
+    with pytest.raises(_lib.GfftError):
+        _lib.plan_query(64, 0, 8, 1)
+
+
+def test_create_nd_argument_errors():
+    """gfft_create_nd checks its arguments before touching a device."""
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    dims = (ctypes.c_uint64 * 3)(64, 64, 64)
+    assert L.gfft_create_nd(ctypes.byref(h), 4, dims, 1, 0, 1, 1) == 5      # rank
+    assert L.gfft_create_nd(ctypes.byref(h), 2, dims, 1, 2, 1, 1) == 3      # real: not multi-dimensional
+    assert L.gfft_create_nd(ctypes.byref(h), 2, dims, 7, 0, 1, 1) == 2      # value type
+    assert L.gfft_create_nd(ctypes.byref(h), 2, dims, 1, 0, 5, 1) == 4      # place
+    assert L.gfft_create_nd(ctypes.byref(h), 2, None, 1, 0, 1, 1) == 7      # null dims
+    big = (ctypes.c_uint64 * 2)(8192, 16)
+    assert L.gfft_create_nd(ctypes.byref(h), 2, big, 1, 0, 1, 1) == 1      # outer axis above one tile
