@@ -425,20 +425,16 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     ins[2] = ws1;
     outs[2] = dst;
   }
-  // one global pass over `nb` transforms (pointers already at the first one)
-  auto run_pass = [&](int g, const void* in_g, void* out_g, long long nb) -> int {
+  for (int g = 0; g < p.nglobal; ++g) {
     const GlobalPass& gp = p.gp[g];
     EngineArgs a;
     std::memset(&a, 0, sizeof(a));
-    unsigned grid_g = 0;  // persistent grid, at most one block per tile
-    a.in = in_g;
-    a.out = out_g;
+    a.in = ins[g];
+    a.out = outs[g];
     a.N = n;
     a.L = gp.L;
     a.stride = n / gp.L;
-    a.nunits = nb * a.stride;
-    grid_g = (unsigned)std::max<long long>(
-        1, std::min<long long>((long long)h->grid[g], (a.nunits + std::max(1, gp.units) - 1) / std::max(1, gp.units)));
+    a.nunits = batch * a.stride;
     a.gNs = gp.Ns;
     a.gB = (long long)p.gtw_B;
     a.gtw_lo = tab + p.gtw_lo_off * esz;
@@ -470,62 +466,38 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     a.scale = (inverse && last) ? 1.0 / (double)n : 1.0;
     a.status = h->d_status;
     if (gp.variant == 6) {
-      a.ntiles = (a.nunits + gp.units - 1) / gp.units;
+      a.ntiles = gp.ntiles;
       a.spin_limit = 1LL << 26;
-      if (gfft_tc_launch(&a, grid_g, (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
-      return GFFT_OK;
+      if (gfft_tc_launch(&a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      continue;
     }
     if (gp.variant == 7) {
-      a.ntiles = (a.nunits + gp.units - 1) / gp.units;
-      if (gfft_mixed_launch(dbl, &a, grid_g, (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
-      return GFFT_OK;
+      a.ntiles = gp.ntiles;
+      if (gfft_mixed_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      continue;
     }
     if (gp.variant == 4 || gp.variant == 5) {
-      a.ntiles = (a.nunits + gp.units - 1) / gp.units;
-      const int e = gp.variant == 4 ? gfft_lane_launch(dbl, &a, grid_g, (unsigned)gp.threads, gp.smem, stream)
-                                    : gfft_lanep2_launch(dbl, &a, grid_g, (unsigned)gp.threads, gp.smem, stream);
+      a.ntiles = gp.ntiles;
+      const int e = gp.variant == 4 ? gfft_lane_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream)
+                                    : gfft_lanep2_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream);
       if (e != 0) return GFFT_E_CUDA;
-      return GFFT_OK;
+      continue;
     }
     if (gp.variant >= 2) {
-      a.ntiles = (a.nunits + gp.units - 1) / gp.units;
+      a.ntiles = gp.ntiles;
       a.stages = gp.stages;
       a.tile_bytes = gp.tile_bytes;
       a.spin_limit = 1LL << 26;
       a.debug_no_issue = 0;
-      const int e = gp.variant == 3 ? gfft_spec_launch(dbl, &a, grid_g, (unsigned)gp.threads, gp.smem, stream)
-                                    : gfft_fast_launch(dbl, &a, grid_g, (unsigned)gp.threads, gp.smem, stream);
+      const int e = gp.variant == 3 ? gfft_spec_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream)
+                                    : gfft_fast_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream);
       if (e != 0) return GFFT_E_CUDA;
-      return GFFT_OK;
+      continue;
     }
     long long grid = (a.nunits + a.W - 1) / a.W;
     if (grid > 0x7FFFFFFFLL) return GFFT_E_INVALID_SIZE;
     if (gfft_engine_launch(dbl, &a, (unsigned)grid, (unsigned)gp.threads, gp.smem, stream) != 0)
       return GFFT_E_CUDA;
-    return GFFT_OK;
-  };
-  // Two-pass complex plans over a large batch run in chunks of about 32 MB:
-  // pass 1 then pass 2 of one chunk, every chunk through the same workspace
-  // region, so that the intermediate is still in L2 when pass 2 reads it and
-  // HBM sees the input read and the output write only.
-  const size_t tbytes = (size_t)n * esz;
-  const bool chunked = p.nglobal == 2 && p.trans < 2 && batch >= 2 && tbytes * (size_t)batch >= (128ull << 20) &&
-                       tbytes <= (16ull << 20);
-  if (chunked) {
-    const long long cb = std::max<long long>(1, (long long)((32ull << 20) / tbytes));
-    for (long long c0 = 0; c0 < batch; c0 += cb) {
-      const long long nb = std::min(cb, batch - c0);
-      const size_t off = (size_t)c0 * tbytes;
-      int st = run_pass(0, (const char*)cur_in + off, ws0, nb);
-      if (st != GFFT_OK) return st;
-      st = run_pass(1, ws0, (char*)dst + off, nb);
-      if (st != GFFT_OK) return st;
-    }
-  } else {
-    for (int g = 0; g < p.nglobal; ++g) {
-      const int st = run_pass(g, ins[g], outs[g], batch);
-      if (st != GFFT_OK) return st;
-    }
   }
   if (p.trans == 2 && !p.real_fused) {
     if (gfft_real_pass_launch(dbl, dst, n, batch, 1, tab + p.rtw_off * esz, stream) != 0) return GFFT_E_CUDA;
