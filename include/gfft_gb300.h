@@ -92,7 +92,8 @@ typedef struct gfft_plan_opts {
                              6 = split-precision tensor-core form (FP32 complex, power-of-two
                                  passes of 64..4096: radix-16 sub-DFTs as FP16 hi/lo matrix
                                  products accumulated in FP32; used only when requested),
-                             7 = column tiles specialised for a mixed-radix pass shape */
+                             7 = column tiles specialised for a mixed-radix pass shape,
+                             8 = one transform per thread-block cluster (N = 2, 4, 8 tiles) */
   int stages;             /* bulk-copy pipeline depth of the fast path (0 = 2) */
   int blocks_per_sm;      /* persistent blocks per SM of the fast path (0 = occupancy) */
   int reserved[4];
@@ -139,7 +140,7 @@ typedef struct gfft_plan_info {
   int threads[4], units[4];    /* launch shape of each pass */
   int kernel_variant[4];       /* 1 generic engine, 2 register-resident fast path, 3 specialised,
                                   4 column tiles, 5 specialised column tiles, 6 tensor-core split,
-                                  7 specialised mixed-radix column tiles */
+                                  7 specialised mixed-radix column tiles, 8 cluster */
   uint64_t workspace_bytes;    /* device scratch owned by the handle */
   uint64_t table_bytes;        /* device twiddle tables owned by the handle */
   int real_fused;              /* real pre/post pass fused into the transform */
