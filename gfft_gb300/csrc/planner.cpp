@@ -254,13 +254,15 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   const long long smem_budget = o.smem_budget > 0 ? o.smem_budget : 160 * 1024;
   auto padded = [&](long long L) { return L + (L >> pad_shift) + 1; };  // spec / fast kernels
   auto epadded = [&](long long L) { return engine_padded(L, dbl); };     // run-time engine kernels
-  // one transform per thread-block cluster (fft_cluster.cu, variant 8):
-  // N = C x M, M = one tile (4096 FP32 / 2048 FP64), C = 2, 4 or 8; the
-  // passes of the length-M plan, then W_N^j for the cross-CTA step
+  // one transform per thread-block cluster (fft_cluster.cu, variant 8), on
+  // request: N = C x M, M = one tile (4096 FP32 / 2048 FP64), C = 2, 4 or 8;
+  // the passes of the length-M plan, then W_N^j for the cross-CTA step.
+  // Slower than the default plans on GB300 (1.2x - 2.5x the time), so not
+  // chosen by default.
   {
     const long long Mcl = dbl ? 2048 : 4096;
     const bool fits = n == 2 * Mcl || n == 4 * Mcl || n == 8 * Mcl;
-    if (fits && trans < 2 && (o.variant == 0 || o.variant == 8) && o.threads == 0 && o.units == 0 &&
+    if (fits && trans < 2 && o.variant == 8 && o.threads == 0 && o.units == 0 &&
         o.radix_order == 0 && o.max_radix == 16 && o.max_pass_len == 0 && o.max_single == 0) {
       HostPlan sub;
       PlanOpts so;

@@ -93,7 +93,8 @@ typedef struct gfft_plan_opts {
                                  passes of 64..4096: radix-16 sub-DFTs as FP16 hi/lo matrix
                                  products accumulated in FP32; used only when requested),
                              7 = column tiles specialised for a mixed-radix pass shape,
-                             8 = one transform per thread-block cluster (N = 2, 4, 8 tiles) */
+                             8 = one transform per thread-block cluster (N = 2, 4, 8 tiles;
+                                 used only when requested) */
   int stages;             /* bulk-copy pipeline depth of the fast path (0 = 2) */
   int blocks_per_sm;      /* persistent blocks per SM of the fast path (0 = occupancy) */
   int reserved[4];

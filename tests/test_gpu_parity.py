@@ -447,7 +447,7 @@ def test_cpp_facade_on_gpu(cuda):
 @pytest.mark.parametrize("dbl", [0, 1])
 @pytest.mark.parametrize("C", [2, 4, 8])
 def test_cluster_kernel(cuda, oracle, C, dbl):
-    """One transform per thread-block cluster (variant 8, N = C tiles):
+    """One transform per thread-block cluster (variant 8 on request, N = C tiles):
     forward and inverse against the exact oracle and the generic engine, in
     place equal to out of place."""
     from gfft_gb300 import _lib
@@ -455,15 +455,16 @@ def test_cluster_kernel(cuda, oracle, C, dbl):
     vt = 0 if dbl else 1
     dt = np.float64 if dbl else np.float32
     B = 3
-    assert _lib.plan_query(n, vt, 0, 1, B)["kernel_variant"] == [8]
+    K8 = {"kernel_variant": 8}
+    assert _lib.plan_query(n, vt, 0, 1, B, K8)["kernel_variant"] == [8]
     x = inputs.gaussian(41 + n, 2 * n * B).astype(dt)
     for tr, sign in ((0, 1), (1, -1)):
-        y = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+        y = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts=K8)
         ex = oracle.fft_ld(x.astype(np.float64), n, B, sign)
         assert rel(y, ex) <= tol(n, dbl), (n, tr, rel(y, ex))
         gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
         assert rel(y, gen) <= tol(n, dbl), (n, tr, rel(y, gen))
-        yi = run_gpu(cuda, n, vt, tr, 0, x, batch=B)
+        yi = run_gpu(cuda, n, vt, tr, 0, x, batch=B, opts=K8)
         assert np.array_equal(y, yi), (n, tr)
 
 
