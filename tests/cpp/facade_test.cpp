@@ -40,6 +40,12 @@ int main(int argc, char** argv) {
   }
   if (DOUBLE::ID != 0 || COMPLEX_FLOAT::ID != 3 || IRDFT::ID != 3 || OpenMP<8>::ID != 7 || IN_PLACE::ID != 0)
     return fail("tag ids");
+  // the cosine-transform tags keep the reference's IDs (src/gfftpolicy.h:302-365)
+  if (DCT1::ID != 4 || IDCT1::ID != 5 || DCT2::ID != 6 || IDCT2::ID != 7 || DCT2::Inverse::ID != 7)
+    return fail("cosine tag ids");
+  typedef GenerateTransform<TYPELIST_1(ulong_<100>), DOUBLE, TYPELIST_2(DCT2, IDCT2), ulong_<1>, Serial, OUT_OF_PLACE>
+      CosineSet;
+  CosineSet cosines;
   if (!gpu) {
     std::printf("facade ok (cpu)\n");
     return 0;
@@ -80,6 +86,26 @@ int main(int argc, char** argv) {
   std::printf("max|dft err|/max|X| = %.3g, roundtrip %.3g, inplace-vs-oop %.3g, inplace roundtrip %.3g\n",
               err / mag, rt, d, rt2);
   if (err / mag > 1e-14 || rt > 1e-10 || d != 0 || rt2 > 1e-10) return fail("accuracy");
+  // DCT2 of 100 reals (the reference's direct.h sum) through the factory
+  {
+    const long M = 100;
+    std::vector<double> a(M), b(M);
+    for (long i = 0; i < M; ++i) a[i] = std::sin(0.37 * i) + 0.25 * i / M;
+    CosineSet::ObjectType* dct = cosines.CreateTransformObject(M, DOUBLE::ID, DCT2::ID, 1, Serial::ID,
+                                                                OUT_OF_PLACE::ID);
+    dct->fft(a.data(), b.data());
+    delete dct;
+    double e2 = 0, m2 = 0;
+    for (long k = 0; k < M; ++k) {
+      long double s2 = 0;
+      for (long l = 0; l < M; ++l)
+        s2 += a[l] * cosl(3.14159265358979323846264338327950288L * (long double)((k * l) % (2 * M)) / M);
+      e2 = std::fmax(e2, std::fabs((double)(s2 - b[k])));
+      m2 = std::fmax(m2, std::fabs((double)s2));
+    }
+    std::printf("dct2 max err / max = %.3g\n", e2 / m2);
+    if (e2 / m2 > 1e-13) return fail("dct2 accuracy");
+  }
   std::printf("facade ok (gpu)\n");
   return 0;
 }
