@@ -200,3 +200,33 @@ def test_create_nd_argument_errors():
     assert L.gfft_create_nd(ctypes.byref(h), 2, None, 1, 0, 1, 1) == 7      # null dims
     big = (ctypes.c_uint64 * 2)(8192, 16)
     assert L.gfft_create_nd(ctypes.byref(h), 2, big, 1, 0, 1, 1) == 1      # outer axis above one tile
+
+
+def _header_shapes():
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gfft_gb300", "csrc",
+                            "mixed_shapes.h")).read()
+    mixed = [tuple(int(v) for v in m.group(2).split(",") if int(v) > 1)
+             for m in re.finditer(r"\{(\d+), \{([\d, ]+)\}\}", src)]
+    ragged = [tuple(int(v) for v in m.group(1).split(",") if int(v) > 1)
+              for m in re.finditer(r"X\(\d+, ([\d, ]+)\)", src)]
+    return mixed, ragged
+
+
+def test_compiled_shapes_are_planner_shapes():
+    """Every compiled pass shape (mixed_shapes.h) is the planner's own radix
+    sequence for its length, so none is unreachable; the mixed-radix column
+    kernel is chosen for each of its single-pass lengths."""
+    mixed, ragged = _header_shapes()
+    assert len(mixed) >= 8 and len(ragged) >= 30
+    for rs in mixed + ragged:
+        L = 1
+        for r in rs:
+            L *= r
+        d = _lib.plan_query(L, 1, 0, 1, 16)
+        assert tuple(d["radices"][0]) == rs, (L, rs, d["radices"])
+    for rs in mixed:
+        L = 1
+        for r in rs:
+            L *= r
+        assert _lib.plan_query(L, 1, 0, 1, 16)["kernel_variant"] == [7], rs
