@@ -166,6 +166,24 @@ def dist_setup(args):
     return world, rank, local
 
 
+def max_over_ranks(total_ms, world, device=None):
+    """The slowest rank's time (every rank's timed region is bracketed by
+    barriers); a tensor on `device` goes through the process group."""
+    if world <= 1:
+        return float(total_ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(total_ms)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(n, batch, world, ms):
+    """Whole-job GFLOP/s: every rank transforms its own batch (replicas, weak
+    scaling), in `ms` per step (the slowest rank's)."""
+    return flops(n, batch) * world / (ms * 1e-3) / 1e9
+
+
 def run_reference(args):
     world, rank, _ = dist_setup(args)
     if rank != 0:
@@ -558,13 +576,9 @@ def main():
     barrier()
     clk = clocks.stop()
     per = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = t.item()
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[-1]), world, dev)
     ms = total_ms / args.steps
-    value = flops(n, batch) * world / (ms * 1e-3) / 1e9
+    value = job_value(n, batch, world, ms)
 
     # roofline of the engine kernel: one launch per step
     launch_ms = statistics.mean(per) / info["kernels_per_exec"]
