@@ -8,10 +8,12 @@ metric = GFLOP/s = 5*N*log2(N)*batch / t (the reference harness's convention,
 test/gfft_performance.h:67-78); the roofline object reports the same launch
 as algorithmic HBM bytes (one read + one write of the data) per second.
 
-`--impl reference` times the reference's algorithm on the host cores: the
-compiled reference cannot run here (it needs the reference tree), so its CPU
-restatement (oracle/gfft_restate.cpp, bit-exact with the compiled reference)
-runs with OpenMP over the batch, all host threads.
+`--impl reference` times the reference itself on the host cores: its serial
+transform objects compiled from its headers (oracle/ref_bench.cpp, built by
+oracle/build.py from the reference checkout or the copy of its headers that
+travels with this tree), OpenMP over the whole batch on every host thread.
+Where it cannot be compiled, the CPU restatement (oracle/gfft_restate.cpp,
+bit-exact with the compiled reference) stands in, labelled "port".
 
 Multi-GPU (torchrun, --gpus N): transforms are independent, so every rank
 runs the same per-GPU batch with no collective on the data path ("weak"
@@ -37,9 +39,10 @@ N = 4096
 BATCH = 65536
 WORKLOAD = "fp32 c2c fft N=4096 x batch 65536, out of place"
 
-# DRAM bytes (read + write) of one launch on this workload: the ncu capture
-# summarised in profiles/spec_kernel_fp32_n4096.md measured 1.0248e9 bytes
-# for batch 16384; traffic scales with the transforms processed (x4).
+# DRAM bytes (read + write) of one launch on this workload: one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum of spec_kernel<float, 4096>)
+# measured 1.0265e9 bytes for batch 16384; traffic scales with the
+# transforms processed (x4).
 NCU_TRAFFIC_BYTES = {(4096, 65536): 4 * 1.0265e9}
 
 
@@ -68,6 +71,8 @@ def parse():
                         "buffers only (small profiling runs)")
     p.add_argument("--suite", action="store_true",
                    help="time every configuration of the workload list (one JSON line each) instead of the headline")
+    p.add_argument("--peaks", action="store_true",
+                   help="measure the CUDA cores' FP64 and FP32 multiply-add peaks (the FP64 configurations' bound)")
     return p.parse_args()
 
 
@@ -137,13 +142,44 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n, batch_sample, reps=3):
-    """The reference's algorithm (CPU restatement) on all host threads over a
-    bounded sample of the workload; min of `reps` runs after one warm-up."""
+def compiled_reference(n, batch, steps, warmup):
+    """The reference itself: its serial transform objects compiled from its
+    headers (oracle/ref_bench.cpp, g++ -O3 -march=native -fopenmp), OpenMP
+    over the batch on every host thread.  Returns (result dict, None) or
+    (None, reason) when it cannot be built on this machine."""
+    from oracle import build as obuild
+    try:
+        exe = obuild.build_ref_bench()
+    except Exception as e:
+        return None, "compiling the reference failed: %s" % str(e).splitlines()[0][:160]
+    if not exe:
+        return None, "the reference's headers are absent on this machine"
+    try:
+        r = subprocess.run([exe, str(n), str(batch), str(steps), str(warmup)], capture_output=True, text=True,
+                           timeout=900)
+    except Exception as e:
+        return None, str(e)[:160]
+    if r.returncode != 0:
+        return None, (r.stderr or r.stdout)[-160:]
+    return json.loads(r.stdout.strip().splitlines()[-1]), None
+
+
+def cpu_baseline(n, batch, reps=3):
+    """CPU baseline of the headline workload: the compiled reference over the
+    whole batch (min of `reps` steps after one warm-up); where it cannot be
+    built, the restatement over a 4096-transform sample."""
+    ref, why = compiled_reference(n, batch, reps, 1)
+    if ref is not None:
+        return {"value": flops(n, batch) / ref["s_min"] / 1e9, "unit": "GFLOP/s", "cores": ref["threads"],
+                "kind": "reference",
+                "sample": "all %d transforms of N=%d fp32 per step, the reference's own Serial objects compiled "
+                          "from its headers (-O3 -march=native), OpenMP over the batch, min of %d steps"
+                          % (batch, n, reps)}
     import numpy as np
 
     from gfft_gb300 import inputs
     from oracle import pyoracle
+    batch_sample = 4096
     x = inputs.uniform(0x5EED0003, 2 * n * batch_sample).astype(np.float32)
     y = np.empty_like(x)
     pyoracle.gfft_batch(n, batch_sample, 1, 0, 1, x, y)
@@ -155,8 +191,8 @@ def cpu_baseline(n, batch_sample, reps=3):
     return {"value": flops(n, batch_sample) / best / 1e9, "unit": "GFLOP/s", "cores": pyoracle.num_threads(),
             "kind": "port",
             "sample": "%d transforms of N=%d fp32 (%.0f MiB), restatement of the reference's serial objects, "
-                      "OpenMP over the batch, min of %d runs" % (batch_sample, n, 8 * n * batch_sample / 2 ** 20,
-                                                                  reps)}
+                      "OpenMP over the batch, min of %d runs (compiled reference unavailable: %s)"
+                      % (batch_sample, n, 8 * n * batch_sample / 2 ** 20, reps, why)}
 
 
 def dist_setup(args):
@@ -185,36 +221,51 @@ def job_value(n, batch, world, ms):
 
 
 def run_reference(args):
+    """The reference arm: the reference's own transform objects on the host
+    cores, for the same workload (the whole batch every step).  Falls back to
+    the restatement (bit-exact with the compiled reference where pinned) on a
+    bounded sample when the reference cannot be compiled here."""
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return
-    from oracle import pyoracle
     n = args.n
-    # a bounded sample per step: about a second of CPU work
-    sample = 4096
-    import numpy as np
+    ref, why = compiled_reference(n, args.batch, args.steps, args.warmup)
+    if ref is not None:
+        dt = ref["s_mean"]
+        v = flops(n, args.batch) / dt / 1e9
+        cpu = {"value": v, "unit": "GFLOP/s", "cores": ref["threads"], "kind": "reference",
+               "sample": "all %d transforms of N=%d fp32 per step; the reference's own Serial objects (%s) "
+                         "compiled from its headers with g++ -O3 -march=native -fopenmp, OpenMP over the batch; "
+                         "its OpenMP<NT> policy does not compile (see oracle/ref_bench.cpp)"
+                         % (args.batch, n, ref["objects"]),
+               "s_min": ref["s_min"]}
+        sample = args.batch
+    else:
+        from oracle import pyoracle
+        sample = 4096
+        import numpy as np
 
-    from gfft_gb300 import inputs
-    x = inputs.uniform(0x5EED0003, 2 * n * sample).astype(np.float32)
-    y = np.empty_like(x)
-    for _ in range(args.warmup):
-        pyoracle.gfft_batch(n, sample, 1, 0, 1, x, y)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        pyoracle.gfft_batch(n, sample, 1, 0, 1, x, y)
-    dt = (time.perf_counter() - t0) / args.steps
-    v = flops(n, sample) / dt / 1e9
-    cores = pyoracle.num_threads()
+        from gfft_gb300 import inputs
+        x = inputs.uniform(0x5EED0003, 2 * n * sample).astype(np.float32)
+        y = np.empty_like(x)
+        for _ in range(args.warmup):
+            pyoracle.gfft_batch(n, sample, 1, 0, 1, x, y)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            pyoracle.gfft_batch(n, sample, 1, 0, 1, x, y)
+        dt = (time.perf_counter() - t0) / args.steps
+        v = flops(n, sample) / dt / 1e9
+        cpu = {"value": v, "unit": "GFLOP/s", "cores": pyoracle.num_threads(), "kind": "port",
+               "sample": "%d of the %d transforms per step; the reference's algorithm restated (bit-exact with the "
+                         "compiled reference), OpenMP over the batch; compiled reference unavailable: %s"
+                         % (sample, args.batch, why)}
     line = {"metric": "C2C FFT GFLOP/s (5Nlog2N/t)", "value": v, "unit": "GFLOP/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1))",
             "impl": "reference",
             "config": {"workload": WORKLOAD, "n": n, "batch": args.batch, "sample_batch": sample,
                        "l2": "inputs larger than L2 not applicable (host)"},
-            "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": cores, "kind": "port",
-                             "sample": "%d of the %d transforms per step; the reference's algorithm restated "
-                                       "(bit-exact with the compiled reference), OpenMP over the batch"
-                                       % (sample, args.batch)},
+            "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -283,6 +334,9 @@ def run_suite(args):
     from gfft_gb300 import inputs
     gfft_gb300.build()
     peak, _ = measured_peaks()
+    fp64_peak = None
+    if any(e[3] == "f64" and (not args.only or args.only in e[0]) for e in SUITE):
+        fp64_peak = fma_peaks()["fp64_fma_gflops"]
     if not args.only or args.only in "c4 ragged":
         run_ragged(args, peak)
     plain_ms = {}
@@ -330,6 +384,11 @@ def run_suite(args):
                 "GB/s_algorithmic": alg_bytes / ms / 1e6, "frac_hbm": alg_bytes / ms / 1e6 / peak,
                 "passes": info["n_global_passes"], "radices": info["radices"], "variant": info["kernel_variant"],
                 "kernels_per_exec": info["kernels_per_exec"], "opts": opts or {}, "inputs": kind}
+        if dbl and fp64_peak:
+            # FP64 transforms: the bound is min(HBM, FP64 pipe); 5 N log2 N against the measured FMA peak
+            line["fp64_fma_gflops"] = fp64_peak
+            line["frac_fp64_peak"] = line["GFLOP/s"] / fp64_peak
+            line["frac_roofline"] = max(line["frac_hbm"], line["frac_fp64_peak"])
         if not opts:
             plain_ms[(n, batch, dt, tr)] = ms
         elif (n, batch, dt, tr) in plain_ms:
@@ -491,6 +550,32 @@ def run_planner(args):
         model.save(os.path.join(args.planner_out, "cost_model.npz"))
 
 
+def fma_peaks():
+    """FP64 and FP32 multiply-add throughput (GFLOP/s) of this GPU, with the
+    SM clocks sampled while the loops run."""
+    from gfft_gb300 import _lib
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    f64 = _lib.measure_fma_peak(1, 1 << 16)
+    f32 = _lib.measure_fma_peak(0, 1 << 18)
+    clk = clocks.stop()
+    return {"fp64_fma_gflops": f64["gflops"], "fp32_fma_gflops": f32["gflops"], "fp64_ms": f64["ms"],
+            "fp32_ms": f32["ms"], "clocks": clk,
+            "how": "gfft_measure_fma_peak: 8 independent FMA chains per thread, every SM at full occupancy, best "
+                   "of 5 launches, CUDA events; 2 flops per FMA"}
+
+
+def run_peaks(args):
+    import gfft_gb300
+    gfft_gb300.build()
+    hbm, kind = measured_peaks()
+    line = fma_peaks()
+    line["hbm_gbs"] = hbm
+    line["hbm_source"] = kind
+    print(json.dumps(line), flush=True)
+
+
 def run_case(args):
     """--case: a plain timing loop over one plan, for profiler captures."""
     import torch
@@ -527,6 +612,9 @@ def main():
         return
     if args.planner:
         run_planner(args)
+        return
+    if args.peaks:
+        run_peaks(args)
         return
     if args.impl == "reference":
         run_reference(args)
@@ -627,7 +715,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(n, 4096)
+            cpu = cpu_baseline(n, batch)
         except Exception as e:  # reported, never fatal
             cpu = {"value": None, "error": str(e)[:200]}
     if rank == 0:

@@ -26,7 +26,8 @@ EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_create_nd", "gfft_exec", "g
             "gfft_exec_noalloc", "gfft_ragged_create", "gfft_ragged_exec", "gfft_ragged_get_info",
             "gfft_ragged_get_status", "gfft_ragged_destroy", "gfft_tune_candidates", "gfft_tune_measure",
             "gfft_plan_features", "gfft_mlp_create", "gfft_mlp_num_params", "gfft_mlp_get_params", "gfft_mlp_set_params",
-            "gfft_mlp_train", "gfft_mlp_predict", "gfft_mlp_gradients", "gfft_mlp_destroy", "gfft_version"]
+            "gfft_mlp_train", "gfft_mlp_predict", "gfft_mlp_gradients", "gfft_mlp_destroy", "gfft_version",
+            "gfft_measure_fma_peak"]
 NFEAT = 24
 
 
@@ -104,6 +105,8 @@ def lib():
         L.gfft_mlp_predict.argtypes = [vp, fp, ci, fp]
         L.gfft_mlp_gradients.argtypes = [vp, fp, fp, ci, fp, fp]
         L.gfft_mlp_destroy.argtypes = [vp]
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.gfft_measure_fma_peak.argtypes = [ci, ci, dp, dp]
         for name in EXPORTED:
             getattr(L, name).restype = getattr(L, name).restype or ci
         L.gfft_strerror.restype = ctypes.c_char_p
@@ -148,3 +151,12 @@ def strerror(status: int) -> str:
 def check(status: int, what: str = ""):
     if status != GFFT_OK:
         raise GfftError(status, what)
+
+
+def measure_fma_peak(dbl: int, iters: int = 1 << 16) -> dict:
+    """Multiply-add throughput of the CUDA cores (FP64 or FP32), best of five
+    timed launches over every SM (gfft_measure_fma_peak)."""
+    g, ms = ctypes.c_double(), ctypes.c_double()
+    check(lib().gfft_measure_fma_peak(int(dbl), int(iters), ctypes.byref(g), ctypes.byref(ms)),
+          "gfft_measure_fma_peak")
+    return {"gflops": g.value, "ms": ms.value, "iters": iters}

@@ -47,6 +47,10 @@ extern "C" int gfft_cluster_launch(int dbl, const EngineArgs* a, int C, long lon
 extern "C" int gfft_tc_setup(size_t max_smem);
 extern "C" int gfft_tc_occupancy(int L, int threads, size_t smem);
 extern "C" int gfft_tc_launch(const EngineArgs* a, unsigned grid, unsigned threads, size_t smem, cudaStream_t stream);
+extern "C" int gfft_col_setup(int dbl, size_t max_smem);
+extern "C" int gfft_col_occupancy(int dbl, int L, int threads, size_t smem);
+extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                               cudaStream_t stream);
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
 
@@ -74,6 +78,7 @@ int setup_device_once(int dbl) {
   if (!dbl && gfft_tc_setup((size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_mixed_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_cluster_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
+  if (gfft_col_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (dev < 64) done[dbl][dev] = true;
   return GFFT_OK;
 }
@@ -200,6 +205,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
   h->parall_id = parall_id;
   h->popts = po;
   h->has_opts = opts != nullptr;
+  h->owns_ws = true;
   int st = setup_device_once(dbl);
   if (st != GFFT_OK) {
     delete h;
@@ -253,6 +259,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)
                        : gp.variant == 7 ? mixed_occupancy(dbl, gp)
+                       : gp.variant == 9 ? gfft_col_occupancy(dbl, gp.L, gp.threads, gp.smem)
                                          : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
       if (gp.variant == 6 && !(opts && opts->blocks_per_sm)) {
         // two blocks fit by registers (launch bound) and shared memory whenever
@@ -289,6 +296,7 @@ int gfft_create(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int
 int gfft_destroy(gfft_handle h) {
   if (!valid(h)) return GFFT_E_INVALID_HANDLE;
   h->magic = 0;
+  if (h->unaligned) gfft_destroy(h->unaligned);
   if (h->dct_inner) gfft_destroy(h->dct_inner);
   if (h->nd_inner) gfft_destroy(h->nd_inner);
   for (int i = 0; i < 2; ++i)
@@ -388,9 +396,11 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     if (gfft_real_pass_launch(dbl, dst, n, batch, 2, tab + p.rtw_off * esz, stream) != 0) return GFFT_E_CUDA;
     cur_in = dst;
   }
-  // buffer sequence of the global passes
-  std::vector<const void*> ins(p.nglobal);
-  std::vector<void*> outs(p.nglobal);
+  // buffer sequence of the global passes (fixed arrays: the allocation-free
+  // entry point runs through here too)
+  const void* ins[GFFT_MAXG] = {};
+  void* outs[GFFT_MAXG] = {};
+  if (p.nglobal < 1 || p.nglobal > GFFT_MAXG) return GFFT_E_INVALID_PLAN;
   const bool inplace = (cur_in == dst);
   if (p.nglobal == 1) {
     ins[0] = cur_in;
@@ -413,8 +423,9 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     }
   } else {
     // in place, odd: in -> ws0 -> ws1 -> dst (the second buffer of an
-    // out-of-place plan called in place is allocated on first need)
-    if (!ws1 && ws0 == h->d_ws[0]) {
+    // out-of-place plan called in place is allocated on first need, only for
+    // handles from gfft_create: any other caller gets GFFT_E_INVALID_PLAN)
+    if (!ws1 && h->owns_ws && ws0 == h->d_ws[0]) {
       if (cudaMalloc(&h->d_ws[1], h->ws_bytes) != cudaSuccess) {
         h->d_ws[1] = nullptr;
         return GFFT_E_ALLOC;
@@ -479,6 +490,13 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
       a.ntiles = gp.ntiles;
       a.spin_limit = 1LL << 26;
       if (gfft_tc_launch(&a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      continue;
+    }
+    if (gp.variant == 9) {
+      a.ntiles = gp.ntiles;
+      a.stages = gp.stages;
+      a.spin_limit = 1LL << 26;
+      if (gfft_col_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
       continue;
     }
     if (gp.variant == 7) {
@@ -584,6 +602,21 @@ int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
   if (h->hp.place == 0 && src != dst) return GFFT_E_INVALID_PLACE;
   if (h->dct_inner) return gfft_dct_exec(h, src, dst, (cudaStream_t)stream);
   if (h->nd_inner) return gfft_nd_exec(h, src, dst, (cudaStream_t)stream);
+  if ((((uintptr_t)src) | ((uintptr_t)dst)) & 15) {
+    bool col = false;
+    for (int g = 0; g < h->hp.nglobal; ++g) col = col || h->hp.gp[g].variant == 9;
+    if (col) {
+      if (!h->unaligned) {
+        gfft_plan_opts o;
+        std::memset(&o, 0, sizeof(o));
+        o.kernel_variant = 5;
+        const int st = gfft_create_opts(&h->unaligned, (uint64_t)h->hp.n, h->vtype, h->trans_id, 1, h->parall_id,
+                                        h->place_id, (uint64_t)h->hp.batch, &o);
+        if (st != GFFT_OK) return st;
+      }
+      return gfft_exec(h->unaligned, src, dst, stream);
+    }
+  }
   return gfft_exec_ws(h, src, dst, (cudaStream_t)stream, h->d_ws[0], h->d_ws[1]);
 }
 

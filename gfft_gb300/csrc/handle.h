@@ -17,6 +17,9 @@ struct gfft_plan {
   size_t tab_bytes = 0;
   void* d_ws[2] = {nullptr, nullptr};
   size_t ws_bytes = 0;
+  // true for handles made by gfft_create: only those may allocate a missing
+  // second workspace on first need (gfft_exec_ws)
+  bool owns_ws = false;
   // staging buffers for gfft_exec_host, allocated on first use
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
@@ -36,6 +39,10 @@ struct gfft_plan {
   cudaEvent_t ev_in[GFFT_MAX_CHUNKS] = {};
   cudaEvent_t ev_done[GFFT_MAX_CHUNKS] = {};
   cudaEvent_t ev_user = nullptr, ev_end = nullptr;
+  // plans with tensor-copy column tiles (variant 9) need 16-byte aligned
+  // buffers: a pointer aligned only to its element runs through this
+  // second handle (column tiles of variant 5), made on first need
+  gfft_plan* unaligned = nullptr;
   // cosine transforms (transform IDs 4-7): pre pass, this inner real
   // transform of length dct_m (complex half-length), post pass
   gfft_plan* dct_inner = nullptr;

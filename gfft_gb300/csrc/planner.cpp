@@ -26,6 +26,8 @@
 #include "plan.h"
 
 bool spec_radices(const GlobalPass& gp);
+// fft_col.cu: launch shape of the tensor-copy column tiles (variant 9)
+extern "C" int gfft_col_shape(int dbl, int L, int stages, int* units, int* threads, size_t* smem);
 
 namespace {
 
@@ -293,11 +295,25 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   while (2 * lane_w * epadded(capL * 2) * esz <= smem_budget) capL *= 2;
   if (o.max_pass_len > 0) capL = std::min<long long>(capL, o.max_pass_len);
 
+  // tensor-copy column tiles (fft_col.cu, variant 9): multi-pass power-of-two
+  // lengths with the default radices; passes of 64 .. 2048 (FP32 up to 4096
+  // when max_pass_len asks for it: two passes for 2^23 / 2^24, whose
+  // 4096-point pass has rows of only two units)
+  const bool col_ok = (n & (n - 1)) == 0 && n < (1LL << 32) && (o.variant == 0 || o.variant == 9) &&
+                      o.threads == 0 && o.units == 0 && o.radix_order == 0 && o.max_radix == 16 &&
+                      o.max_single == 0 && o.smem_budget == 0;
+  const long long col_max = dbl ? 2048 : 4096;
+  long long col_cap = 2048;
+  if (o.max_pass_len > 0) col_cap = std::min<long long>(o.max_pass_len, col_max);
+
   std::vector<long long> Ls;
   if (n <= cap1) {
     Ls.push_back(n);
   } else {
     bool ok = false;
+    if (col_ok && col_cap >= 64) {
+      for (int P = 2; P <= GFFT_MAXG && !ok; ++P) ok = split_passes(n, P, col_cap, Ls) && Ls.back() >= 64;
+    }
     for (int P = 2; P <= GFFT_MAXG && !ok; ++P) ok = split_passes(n, P, capL, Ls);
     if (!ok) return 1;  // a prime factor larger than one block can hold
   }
@@ -445,6 +461,24 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       gp.ntiles = (batch * (n / gp.L) + W - 1) / W;
       // aligned operands (1 KB slack, 32 KB A, 4 KB B), two padded buffers, mbarrier and TMEM slot
       gp.smem = (size_t)(1024 + 32768 + 4096 + 2 * W * padded(gp.L) * 8 + 16);
+    }
+    // tensor-copy column tiles: every tile of W units lies in one transform
+    // (W divides N / L) and maps to W consecutive outputs (W divides Ns)
+    if (col_ok && plan.nglobal > 1 && gp.L >= 64 && gp.L <= col_max && spec_radices(gp)) {
+      int W = 0, T = 0;
+      size_t sm = 0;
+      int S = o.stages > 0 ? o.stages : 2;
+      if (gfft_col_shape(dbl, gp.L, S, &W, &T, &sm) == 0 && (n / gp.L) % W == 0 && (g == 0 || Ns % W == 0)) {
+        while (S > 1 && sm > 227 * 1024) gfft_col_shape(dbl, gp.L, --S, &W, &T, &sm);
+        if (sm <= 227 * 1024) {
+          gp.variant = 9;
+          gp.units = W;
+          gp.threads = T;
+          gp.stages = S;
+          gp.smem = sm;
+          gp.ntiles = batch * (n / gp.L) / W;
+        }
+      }
     }
     // length-specialised variant: default radix order, L in the compiled set
     bool spec = gp.variant == 2 && (o.variant == 0 || o.variant == 3) && o.units == 0 && o.threads == 0 &&

@@ -94,7 +94,10 @@ typedef struct gfft_plan_opts {
                                  products accumulated in FP32; used only when requested),
                              7 = column tiles specialised for a mixed-radix pass shape,
                              8 = one transform per thread-block cluster (N = 2, 4, 8 tiles;
-                                 used only when requested) */
+                                 used only when requested),
+                             9 = column tiles moved by 2-D tensor copies (passes of 64..4096
+                                 of a multi-pass power-of-two length; device buffers
+                                 16-byte aligned, others run through variant 5) */
   int stages;             /* bulk-copy pipeline depth of the fast path (0 = 2) */
   int blocks_per_sm;      /* persistent blocks per SM of the fast path (0 = occupancy) */
   int reserved[4];
@@ -141,7 +144,8 @@ typedef struct gfft_plan_info {
   int threads[4], units[4];    /* launch shape of each pass */
   int kernel_variant[4];       /* 1 generic engine, 2 register-resident fast path, 3 specialised,
                                   4 column tiles, 5 specialised column tiles, 6 tensor-core split,
-                                  7 specialised mixed-radix column tiles, 8 cluster */
+                                  7 specialised mixed-radix column tiles, 8 cluster,
+                                  9 column tiles moved by 2-D tensor copies */
   uint64_t workspace_bytes;    /* device scratch owned by the handle */
   uint64_t table_bytes;        /* device twiddle tables owned by the handle */
   int real_fused;              /* real pre/post pass fused into the transform */
@@ -253,6 +257,14 @@ int gfft_ragged_destroy(gfft_ragged* handle);
  * without ordering -- race on it and must be serialised by the caller. */
 int gfft_exec_noalloc(uint64_t n, int vtype_id, int trans_id, uint64_t batch, const void* src, void* dst,
                       gfft_stream stream);
+
+/* Multiply-add throughput of the CUDA cores in GFLOP/s (2 flops per FMA),
+ * FP64 (dbl = 1) or FP32: eight independent chains per thread over every
+ * SM, best of five launches of `iters` iterations, CUDA events.  The FP64
+ * figure bounds the FP64 transforms (FP64 is a small fraction of GB300's
+ * FP32 rate).  No reference counterpart (its harness reports
+ * 5 N log2 N / t only, test/gfft_performance.h:67-78). */
+int gfft_measure_fma_peak(int dbl, int iters, double* gflops, double* ms);
 
 /* Library version string. */
 const char* gfft_version(void);

@@ -20,9 +20,18 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("GFFT_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $GFFT_REFERENCE_ROOT, else a directory named
+# `reference` beside this repository's checkout; absent on machines that only
+# run the prebuilt fixtures.
+REF_ROOT = os.environ.get("GFFT_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libgfftref.so")
+# a copy of the reference's headers (src/*.h, loki/*.h), made where the
+# checkout exists, for machines that have only this working tree
+# (git-ignored, never committed)
+REF_STAGE = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "gfft")
+REF_BENCH = os.path.join(HERE, "_ref", "ref_bench")
 
 _CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fopenmp"]
 
@@ -84,6 +93,54 @@ def build_ref(force: bool = False) -> str | None:
     _run(["g++", "-shared", *objs, "-o", tmp])
     os.replace(tmp, REF_SO)
     return REF_SO
+
+
+def stage_ref() -> str | None:
+    """Copy the reference's headers next to this tree (baseline/_ref/gfft),
+    so that the benchmark's CPU arm can compile the reference where the
+    checkout is absent.  Does nothing without the checkout."""
+    if not os.path.isdir(os.path.join(REF_ROOT, "src")):
+        return None
+    for sub in ("src", "loki"):
+        src = os.path.join(REF_ROOT, sub)
+        dst = os.path.join(REF_STAGE, sub)
+        os.makedirs(dst, exist_ok=True)
+        for f in os.listdir(src):
+            if f.endswith(".h"):
+                shutil.copy2(os.path.join(src, f), os.path.join(dst, f))
+    return REF_STAGE
+
+
+def ref_include() -> list | None:
+    """Include flags of the reference: the checkout if present, else the
+    staged copy; None when neither exists."""
+    for root in (REF_ROOT, REF_STAGE):
+        if os.path.isdir(os.path.join(root, "src")) and os.path.isdir(os.path.join(root, "loki")):
+            return ["-I", os.path.join(HERE, "refshim"), "-I", os.path.join(root, "src"), "-I",
+                    os.path.join(root, "loki")]
+    return None
+
+
+def build_ref_bench(force: bool = False) -> str | None:
+    """Compile ref_bench.cpp (the reference's serial objects, OpenMP over the
+    batch) with -O3 -march=native -fopenmp into oracle/_ref/ref_bench; plain
+    -O3 where the compiler rejects -march=native.  None without the
+    reference's headers."""
+    inc = ref_include()
+    if inc is None:
+        return None
+    drv = os.path.join(HERE, "ref_bench.cpp")
+    if not force and not _stale(REF_BENCH, [drv, __file__]):
+        return REF_BENCH
+    os.makedirs(os.path.dirname(REF_BENCH), exist_ok=True)
+    base = ["g++", "-std=c++14", "-O3", "-fopenmp", "-w", "-ftemplate-depth=100000", *inc, drv, "-o",
+            REF_BENCH + ".tmp"]
+    try:
+        _run(base[:3] + ["-march=native"] + base[3:])
+    except RuntimeError:
+        _run(base)
+    os.replace(REF_BENCH + ".tmp", REF_BENCH)
+    return REF_BENCH
 
 
 if __name__ == "__main__":

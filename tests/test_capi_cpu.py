@@ -76,18 +76,32 @@ def test_plan_power_of_two_uses_radix16():
 
 
 def test_plan_column_kernel_selection():
-    """Power-of-two passes of 64..1024 take the length-specialised column
-    tiles (5); other lengths, explicit options and short transforms keep the
-    prefetching column tiles (4)."""
-    for n, vt in ((1 << 16, 1), (1 << 20, 1), (1 << 24, 1), (1 << 20, 0), (1 << 22, 0)):
+    """Multi-pass power-of-two lengths take the tensor-copy column tiles (9)
+    with passes of 64..2048 (two passes up to 2^22); on request, power-of-two
+    passes of 64..1024 take the length-specialised column tiles (5); other
+    lengths, explicit options and short transforms keep the prefetching
+    column tiles (4)."""
+    for n, vt, passes in ((1 << 13, 0, 2), (1 << 16, 1, 2), (1 << 20, 1, 2), (1 << 22, 1, 2), (1 << 24, 1, 3),
+                          (1 << 20, 0, 2), (1 << 22, 0, 2), (1 << 27, 1, 3)):
         d = _lib.plan_query(n, vt, 0, 1, 1)
+        assert d["n_global_passes"] == passes and set(d["kernel_variant"]) == {9}, (n, vt, d)
+        assert all(64 <= L <= 2048 for L in d["pass_len"][:passes])
+        # tiles of about 64 KB: units = 64 KB / (L * element size), 2 .. 64
+        esz = 16 if vt == 0 else 8
+        for L, W in zip(d["pass_len"][:passes], d["units"][:passes]):
+            assert W == max(2, min(64, 65536 // esz // L)), (L, W)
+    # two passes of 4096 x 4096 on request
+    d = _lib.plan_query(1 << 24, 1, 0, 1, 1, {"max_pass_len": 4096})
+    assert d["pass_len"][:2] == [4096, 4096] and d["kernel_variant"][:2] == [9, 9], d
+    for n, vt in ((1 << 16, 1), (1 << 20, 1), (1 << 24, 1), (1 << 20, 0), (1 << 22, 0)):
+        d = _lib.plan_query(n, vt, 0, 1, 1, {"kernel_variant": 5})
         assert d["n_global_passes"] >= 2 and set(d["kernel_variant"]) == {5}, (n, vt, d)
         assert all(64 <= L <= 1024 for L in d["pass_len"])
     assert set(_lib.plan_query(5 ** 8 * 3, 1, 0, 1, 1)["kernel_variant"]) <= {4, 7}
     assert set(_lib.plan_query(1 << 20, 1, 0, 1, 1, {"kernel_variant": 4})["kernel_variant"]) == {4}
     assert set(_lib.plan_query(1 << 20, 1, 0, 1, 1, {"max_radix": 8})["kernel_variant"]) == {4}
     # an 8192-point FP64 transform of two 64 x 128 passes: tile (2048) divides n
-    d = _lib.plan_query(8192, 0, 0, 1, 1, {"max_pass_len": 128})
+    d = _lib.plan_query(8192, 0, 0, 1, 1, {"max_pass_len": 128, "kernel_variant": 5})
     assert set(d["kernel_variant"]) == {5}, d
     # 1024 points in two passes: a 2048-value tile would span transforms
     d = _lib.plan_query(1024, 0, 0, 1, 4, {"max_pass_len": 64})

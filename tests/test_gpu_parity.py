@@ -497,14 +497,14 @@ def test_mixed_columns(cuda, oracle, n, B, dbl):
                                          (1 << 24, 0, 1, 0), (1 << 18, 0, 2, 64), (1 << 12, 1, 5, 64),
                                          (1 << 18, 1, 2, 0), (1 << 22, 1, 1, 0), (1 << 15, 0, 3, 256)])
 def test_multipass_spec_columns(cuda, oracle, n, dbl, B, cap):
-    """The length-specialised column-tile kernel (variant 5, chosen by default
-    for power-of-two passes of 64..1024) against the generic engine and the
-    prefetching column-tile kernel, forward and inverse, out of place and in
-    place, and against the exact oracle."""
+    """The length-specialised column-tile kernel (variant 5, for power-of-two
+    passes of 64..1024) against the generic engine and the prefetching
+    column-tile kernel, forward and inverse, out of place and in place, and
+    against the exact oracle."""
     from gfft_gb300 import _lib
     vt = 0 if dbl else 1
     dt = np.float64 if dbl else np.float32
-    base = {"max_pass_len": cap} if cap else {}
+    base = {"max_pass_len": cap, "kernel_variant": 5} if cap else {"kernel_variant": 5}
     info = _lib.plan_query(n, vt, 0, 1, B, base or None)
     assert info["n_global_passes"] >= 2 and all(v == 5 for v in info["kernel_variant"]), info
     x = inputs.gaussian(17 + n, 2 * n * B).astype(dt)
