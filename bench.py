@@ -291,34 +291,61 @@ SUITE = [
 
 def run_ragged(args, peak):
     """C4: 10,000 FP32 transforms, lengths log-uniform in 2^6..2^18 snapped to
-    5-smooth values, one persistent launch replayed from a CUDA graph."""
+    5-smooth values, one persistent launch replayed from a CUDA graph, with
+    the planner's default schedule and with the autotuner's measured
+    schedule (tuner.ragged_schedule); beside them, the same transforms as
+    one launch per distinct length (batched transform objects)."""
     import torch
 
     from gfft_gb300 import gfft as G
-    from gfft_gb300 import inputs
+    from gfft_gb300 import inputs, tuner
     sizes = inputs.ragged_sizes(0x5EED0004, args.ragged_count, 6, 18)
     total = int(sizes.sum())
     x = torch.rand(2 * total, device="cuda", dtype=torch.float32).mul_(2).sub_(1)
     y = torch.empty_like(x)
-    rb = G.RaggedBatch(sizes, G.FLOAT, G.DFT)
-    for _ in range(3):
-        rb.fft(x, y)
-    torch.cuda.synchronize()
-    steps = 20
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
-        rb.fft(x, y)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
     fl = float(sum(5.0 * n * math.log2(n) for n in sizes if n > 1))
     alg = 16.0 * total
+
+    def timed(fn, steps=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    rb = G.RaggedBatch(sizes, G.FLOAT, G.DFT)
+    ms = timed(lambda: rb.fft(x, y))
+    t0 = time.perf_counter()
+    sched = tuner.ragged_schedule(sizes, 1, 0)
+    tune_s = time.perf_counter() - t0
+    rt = G.RaggedBatch(sizes, G.FLOAT, G.DFT, schedule=sched)
+    ms_tuned = timed(lambda: rt.fft(x, y))
+    # one launch per distinct length over contiguous copies of its transforms
+    import numpy as np
+    lengths, counts = np.unique(sizes, return_counts=True)
+    objs = []
+    for n, c in zip(lengths, counts):
+        n, c = int(n), int(c)
+        xs = torch.rand(2 * n * c, device="cuda", dtype=torch.float32)
+        objs.append((G.TransformObject(n, G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, c), xs, torch.empty_like(xs)))
+
+    def separate():
+        for o, a, b in objs:
+            o.fft(a, b)
+    ms_sep = timed(separate, steps=5)
     info = rb.info()
     line = {"config": "c4 fp32 ragged %d lengths 2^6..2^18 (5-smooth), one persistent launch, graph replay"
                       % len(sizes),
             "transforms": len(sizes), "total_points": total, "ms": ms, "GFLOP/s": fl / ms / 1e6,
-            "GB/s_algorithmic": alg / ms / 1e6, "frac_hbm": alg / ms / 1e6 / peak, "status": rb.status(), **info}
+            "GB/s_algorithmic": alg / ms / 1e6, "frac_hbm": alg / ms / 1e6 / peak,
+            "ms_tuned_schedule": ms_tuned, "frac_hbm_tuned": alg / ms_tuned / 1e6 / peak,
+            "tuned_lengths": len(sched), "tuning_s": tune_s,
+            "ms_one_launch_per_length": ms_sep, "status": rb.status(), "status_tuned": rt.status(), **info}
     print(json.dumps(line), flush=True)
 
 

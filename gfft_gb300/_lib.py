@@ -23,7 +23,7 @@ STATUS_NAMES = {
 # every symbol the header declares, checked by the CPU tests
 EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_create_nd", "gfft_exec", "gfft_exec_host", "gfft_destroy", "gfft_strerror",
             "gfft_get_info", "gfft_plan_query", "gfft_get_device_status", "gfft_selftest_bounded_wait",
-            "gfft_exec_noalloc", "gfft_ragged_create", "gfft_ragged_exec", "gfft_ragged_get_info",
+            "gfft_exec_noalloc", "gfft_ragged_create", "gfft_ragged_create_opts", "gfft_ragged_get_plan", "gfft_ragged_exec", "gfft_ragged_get_info",
             "gfft_ragged_get_status", "gfft_ragged_destroy", "gfft_tune_candidates", "gfft_tune_measure",
             "gfft_plan_features", "gfft_mlp_create", "gfft_mlp_num_params", "gfft_mlp_get_params", "gfft_mlp_set_params",
             "gfft_mlp_train", "gfft_mlp_predict", "gfft_mlp_gradients", "gfft_mlp_destroy", "gfft_version",
@@ -35,7 +35,7 @@ class PlanOpts(ctypes.Structure):
     _fields_ = [("radix_order", ctypes.c_int), ("max_radix", ctypes.c_int), ("threads_per_block", ctypes.c_int),
                 ("units_per_block", ctypes.c_int), ("max_pass_len", ctypes.c_int),
                 ("kernel_variant", ctypes.c_int), ("stages", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("reserved", ctypes.c_int * 4)]
+                ("decimation", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -88,6 +88,9 @@ def lib():
         L.gfft_selftest_bounded_wait.argtypes = [ctypes.c_longlong, ctypes.POINTER(ci)]
         L.gfft_exec_noalloc.argtypes = [u64, ci, ci, u64, vp, vp, vp]
         L.gfft_ragged_create.argtypes = [ctypes.POINTER(vp), u64, ctypes.POINTER(u64), ci, ci]
+        L.gfft_ragged_create_opts.argtypes = [ctypes.POINTER(vp), u64, ctypes.POINTER(u64), ci, ci, u64,
+                                              ctypes.POINTER(u64), ctypes.POINTER(PlanOpts)]
+        L.gfft_ragged_get_plan.argtypes = [vp, u64, ctypes.POINTER(PlanInfo)]
         L.gfft_ragged_exec.argtypes = [vp, vp, vp, vp]
         L.gfft_ragged_get_info.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(ci),
                                            ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_uint)]

@@ -70,6 +70,42 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
   }
 }
 
+// The same pass transposed (decimation in frequency): gather the R legs
+// from the positions the decimation-in-time pass writes, butterfly, then
+// twiddle output r by W_(Ns R)^(k r) and scatter to the positions the
+// decimation-in-time pass reads.  The DFT matrix is symmetric, so running
+// the transposed passes in reverse order computes the same transform: the
+// autosort (Stockham) form of the reference's frequency-decimation
+// recursion InFreq / T_DFTk_x_Im (src/gfftalgfreq.h:106-432).
+template <typename T, int R>
+__device__ __forceinline__ void block_pass_dif(const typename Vec<T>::t* __restrict__ src,
+                                               typename Vec<T>::t* __restrict__ dst, const EngineArgs& a,
+                                               const BlockPass& p, const typename Vec<T>::t* __restrict__ tw) {
+  typedef typename Vec<T>::t V;
+  const int L = a.L;
+  const int nb = L / R;
+  const int total = a.W * nb;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int lane = (int)fdiv((unsigned)i, p.fd_nb);
+    const int j = i - lane * nb;
+    const int k = j - (int)fdiv((unsigned)j, p.fd_ns) * p.Ns;
+    const int base = (j - k) * R + k;
+    const V* s = src + lane * a.Lp;
+    V* d = dst + lane * a.Lp;
+    V v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[pad<T>(base + r * p.Ns)];
+    dft<T, V, R>(v);
+    if (p.Ns > 1) {
+      const V* t = tw + p.tw + k;
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(t + (r - 1) * p.Ns));
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[pad<T>(j + r * nb)] = v[r];
+  }
+}
+
 // generic odd prime radix: every output sums R twiddled inputs (O(R^2))
 template <typename T>
 __device__ void block_pass_generic(const typename Vec<T>::t* __restrict__ src, typename Vec<T>::t* __restrict__ dst,
@@ -97,6 +133,38 @@ __device__ void block_pass_generic(const typename Vec<T>::t* __restrict__ src, t
       if (m >= R) m -= R;
     }
     d[pad<T>((j - k) * R + k + q * p.Ns)] = acc;
+  }
+}
+
+// the generic prime pass transposed: output q = W_(Ns R)^(k q) * sum_r
+// x[(j - k) R + k + r Ns] W_R^(r q), written to j + q nb
+template <typename T>
+__device__ void block_pass_generic_dif(const typename Vec<T>::t* __restrict__ src,
+                                       typename Vec<T>::t* __restrict__ dst, const EngineArgs& a, const BlockPass& p,
+                                       const typename Vec<T>::t* __restrict__ tw) {
+  typedef typename Vec<T>::t V;
+  const int L = a.L, R = p.R;
+  const int nb = L / R;
+  const int total = a.W * L;  // one output per iteration
+  const V* wr = tw + p.gen;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int lane = i / L;
+    const int rem = i - lane * L;
+    const int q = rem / nb;  // output leg
+    const int j = rem - q * nb;
+    const V* s = src + lane * a.Lp;
+    V* d = dst + lane * a.Lp;
+    const int k = j % p.Ns;
+    const int base = (j - k) * R + k;
+    V acc = mk<V>(0, 0);
+    int m = 0;  // (r*q) mod R
+    for (int r = 0; r < R; ++r) {
+      acc = cadd(acc, cmul(s[pad<T>(base + r * p.Ns)], __ldg(wr + m)));
+      m += q;
+      if (m >= R) m -= R;
+    }
+    if (p.Ns > 1 && q > 0) acc = cmul(acc, __ldg(tw + p.tw + (q - 1) * p.Ns + k));
+    d[pad<T>(j + q * nb)] = acc;
   }
 }
 
@@ -199,6 +267,37 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
         buf[lane * a.Lp + pad<T>(s)] = a.conj ? cconj(v[q]) : v[q];
       }
     }
+  } else if (a.dif) {
+    // lane units of a frequency-decimation pass: gather from the positions
+    // the time-decimation pass writes (t N + (b - k) L + k + s Ns); the
+    // twiddle comes after the butterflies (store_tile)
+    const int W = a.W;
+    const int lane = threadIdx.x % W;
+    const int sstep = blockDim.x / W;
+    const long long u = u0 + lane;
+    V* bl = buf + lane * a.Lp;
+    if (u >= a.nunits) {
+      for (int s = threadIdx.x / W; s < L; s += sstep) bl[pad<T>(s)] = mk<V>(0, 0);
+      return;
+    }
+    const long long t = u / a.stride;
+    const long long b = u - t * a.stride;
+    const long long k = b % a.gNs;
+    const V* src = in + t * a.N + (b - k) * L + k;
+    for (int s0 = threadIdx.x / W; s0 < L; s0 += 8 * sstep) {
+      V v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int s = s0 + q * sstep;
+        if (s < L) v[q] = src[(long long)s * a.gNs];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int s = s0 + q * sstep;
+        if (s >= L) break;
+        bl[pad<T>(s)] = a.conj ? cconj(v[q]) : v[q];
+      }
+    }
   } else {
     // lane units: the block's threads are a whole number of W-groups, so
     // each thread keeps one lane and walks its samples
@@ -299,6 +398,28 @@ __device__ __forceinline__ void store_tile(const EngineArgs& a, const typename V
       V v = buf[lane * a.Lp + pad<T>(s)];
       if (a.conj) v = cconj(v);
       tile[i] = cscale(v, sc);
+    }
+  } else if (a.dif) {
+    // lane units of a frequency-decimation pass: the four-step twiddle of
+    // sample s, then scatter to the positions the time-decimation pass
+    // reads (t N + b + s N/L)
+    const int W = a.W;
+    const int lane = threadIdx.x % W;
+    const int sstep = blockDim.x / W;
+    const long long u = u0 + lane;
+    if (u >= a.nunits) return;
+    const long long t = u / a.stride;
+    const long long b = u - t * a.stride;
+    const long long k = b % a.gNs;
+    const long long kstep = a.notw ? 0 : k * (a.N / (a.gNs * L));
+    const int lgB = 63 - __clzll(a.gB);
+    V* dstp = out + t * a.N + b;
+    const V* bl = buf + lane * a.Lp;
+    for (int s = threadIdx.x / W; s < L; s += sstep) {
+      V v = bl[pad<T>(s)];
+      if (kstep) v = cmul(v, global_twiddle<T>(a, kstep * s, lgB));
+      if (a.conj) v = cconj(v);
+      dstp[(long long)s * a.stride] = cscale(v, sc);
     }
   } else if (a.gNs == 1) {
     // first global pass: lane b's outputs are the L contiguous elements at

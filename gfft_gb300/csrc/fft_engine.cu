@@ -29,6 +29,33 @@ __global__ void __launch_bounds__(512) engine_kernel(const __grid_constant__ Eng
   __syncthreads();
   V* src = b0;
   V* dst = b1;
+  if (a.dif) {
+    // frequency decimation: the transposed passes in reverse order
+    for (int p = a.npass - 1; p >= 0; --p) {
+      const BlockPass bp = a.pass[p];
+      switch (bp.R) {
+        case 16: block_pass_dif<T, 16>(src, dst, a, bp, tw); break;
+        case 8: block_pass_dif<T, 8>(src, dst, a, bp, tw); break;
+        case 4: block_pass_dif<T, 4>(src, dst, a, bp, tw); break;
+        case 2: block_pass_dif<T, 2>(src, dst, a, bp, tw); break;
+        case 3: block_pass_dif<T, 3>(src, dst, a, bp, tw); break;
+        case 5: block_pass_dif<T, 5>(src, dst, a, bp, tw); break;
+        case 7: block_pass_dif<T, 7>(src, dst, a, bp, tw); break;
+        case 6: block_pass_dif<T, 6>(src, dst, a, bp, tw); break;
+        case 9: block_pass_dif<T, 9>(src, dst, a, bp, tw); break;
+        case 10: block_pass_dif<T, 10>(src, dst, a, bp, tw); break;
+        case 12: block_pass_dif<T, 12>(src, dst, a, bp, tw); break;
+        case 15: block_pass_dif<T, 15>(src, dst, a, bp, tw); break;
+        default: block_pass_generic_dif<T>(src, dst, a, bp, tw); break;
+      }
+      __syncthreads();
+      V* t = src;
+      src = dst;
+      dst = t;
+    }
+    store_tile<T>(a, src, u0);
+    return;
+  }
   for (int p = 0; p < a.npass; ++p) {
     const BlockPass bp = a.pass[p];
     switch (bp.R) {

@@ -48,7 +48,7 @@ extern "C" int gfft_tc_setup(size_t max_smem);
 extern "C" int gfft_tc_occupancy(int L, int threads, size_t smem);
 extern "C" int gfft_tc_launch(const EngineArgs* a, unsigned grid, unsigned threads, size_t smem, cudaStream_t stream);
 extern "C" int gfft_col_setup(int dbl, size_t max_smem);
-extern "C" int gfft_col_occupancy(int dbl, int L, int threads, size_t smem);
+extern "C" int gfft_col_occupancy(int dbl, int L, int rf, int threads, size_t smem);
 extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                cudaStream_t stream);
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
@@ -115,6 +115,9 @@ int parse_opts(const gfft_plan_opts* opts, PlanOpts& po) {
   if (opts->stages < 0 || opts->stages > 8 || opts->blocks_per_sm < 0 || opts->blocks_per_sm > 32)
     return GFFT_E_INVALID_PLAN;
   po.stages = opts->stages;
+  if (opts->decimation < 0 || opts->decimation > 1) return GFFT_E_INVALID_PLAN;
+  if (opts->decimation && opts->kernel_variant && opts->kernel_variant != 1) return GFFT_E_INVALID_PLAN;
+  po.dif = opts->decimation;
   return GFFT_OK;
 }
 
@@ -259,7 +262,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)
                        : gp.variant == 7 ? mixed_occupancy(dbl, gp)
-                       : gp.variant == 9 ? gfft_col_occupancy(dbl, gp.L, gp.threads, gp.smem)
+                       : gp.variant == 9 ? gfft_col_occupancy(dbl, gp.L, gp.rf, gp.threads, gp.smem)
                                          : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
       if (gp.variant == 6 && !(opts && opts->blocks_per_sm)) {
         // two blocks fit by registers (launch bound) and shared memory whenever
@@ -440,12 +443,17 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     ins[2] = ws1;
     outs[2] = dst;
   }
-  for (int g = 0; g < p.nglobal; ++g) {
+  // step `step` runs global pass `step` (time decimation) or
+  // nglobal - 1 - step (frequency decimation: the transposed passes, last
+  // to first)
+  for (int step = 0; step < p.nglobal; ++step) {
+    const int g = p.dif ? p.nglobal - 1 - step : step;
     const GlobalPass& gp = p.gp[g];
     EngineArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.in = ins[g];
-    a.out = outs[g];
+    a.in = ins[step];
+    a.out = outs[step];
+    a.dif = p.dif;
     a.N = n;
     a.L = gp.L;
     a.stride = n / gp.L;
@@ -471,7 +479,7 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     }
     a.fd_L = make_fastdiv((unsigned)gp.L);
     a.fd_half = make_fastdiv((unsigned)(gp.L / 2 + 1));
-    const bool last = (g == p.nglobal - 1);
+    const bool last = (step == p.nglobal - 1);
     a.real = p.real_fused ? ((p.trans == 2) ? 1 : 2) : 0;
     // The inverse runs as conj(FFT(conj x)) / N.  Every pass conjugates on
     // load and on store: the pairs cancel between passes, so the inter-pass
@@ -493,6 +501,8 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
       continue;
     }
     if (gp.variant == 9) {
+      a.real = gp.rf;
+      a.ftw = p.ftw_off[g] ? (const void*)(tab + p.ftw_off[g] * esz) : nullptr;
       a.ntiles = gp.ntiles;
       a.stages = gp.stages;
       a.spin_limit = 1LL << 26;
@@ -645,6 +655,7 @@ static int exec_host_chunked(gfft_handle h, const void* src, void* dst, cudaStre
     o.max_pass_len = h->popts.max_pass_len;
     o.kernel_variant = h->popts.variant;
     o.stages = h->popts.stages;
+    o.decimation = h->popts.dif;
     const gfft_plan_opts* op = h->has_opts ? &o : nullptr;
     int st = gfft_create_opts(&h->chunk_plan[0], (uint64_t)n, h->vtype, h->trans_id, 1, h->parall_id, h->place_id,
                               (uint64_t)cb, op);

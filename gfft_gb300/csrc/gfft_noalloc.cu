@@ -29,7 +29,10 @@
 //
 // Set-up: the first call on each device (with that device current) looks up
 // the array's device address with cudaGetSymbolAddress and sets the engine
-// kernel's shared-memory limit; make that first call before any stream
+// kernel's shared-memory limit.  With CUDA's lazy module loading (the
+// default), that lookup is what loads this translation unit's module on the
+// device and reserves the array (about 65 MiB), and it may synchronise the
+// device; callers make one warm-up call at start-up, before any stream
 // capture on that device.
 #include <cuda_runtime.h>
 

@@ -235,6 +235,8 @@ struct gfft_ragged {
   const void* g_src = nullptr;
   void* g_dst = nullptr;
   int max_passes = 1;
+  // host copy of the per-length plans (gfft_ragged_get_plan)
+  std::vector<RaggedPlan> hplans;
   unsigned magic = 0x6A66ED00u;
 };
 
@@ -269,11 +271,24 @@ int upload(void** dst, const std::vector<T>& v) {
 extern "C" {
 
 int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* sizes, int vtype_id, int trans_id) {
+  return gfft_ragged_create_opts(handle, count, sizes, vtype_id, trans_id, 0, nullptr, nullptr);
+}
+
+int gfft_ragged_create_opts(gfft_ragged** handle, uint64_t count, const uint64_t* sizes, int vtype_id, int trans_id,
+                            uint64_t n_opts, const uint64_t* opt_lengths, const gfft_plan_opts* opts) {
   if (!handle || !sizes) return GFFT_E_NULL_POINTER;
   *handle = nullptr;
   if (count == 0 || count > (1ULL << 31)) return GFFT_E_INVALID_SIZE;
   if (vtype_id < 0 || vtype_id > 3) return GFFT_E_INVALID_TYPE;
   if (trans_id != 0 && trans_id != 1) return GFFT_E_INVALID_TRANSFORM;
+  if (n_opts && (!opt_lengths || !opts)) return GFFT_E_NULL_POINTER;
+  for (uint64_t i = 0; i < n_opts; ++i) {
+    const gfft_plan_opts& o = opts[i];
+    if (o.radix_order < 0 || o.radix_order > 2 || o.units_per_block < 0 || o.units_per_block > 256 ||
+        o.max_pass_len < 0 || (o.max_radix && o.max_radix != 2 && o.max_radix != 4 && o.max_radix != 8 &&
+                               o.max_radix != 16))
+      return GFFT_E_INVALID_PLAN;
+  }
   gfft_ragged* r = new (std::nothrow) gfft_ragged();
   if (!r) return GFFT_E_ALLOC;
   r->dbl = (vtype_id == 0 || vtype_id == 2) ? 1 : 0;
@@ -307,8 +322,20 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
   std::vector<double> tab;
   int lanes_max = 0;
   for (size_t d = 0; d < distinct.size(); ++d) {
+    // this length's schedule: the caller's options (the autotuner's choice), else the defaults
+    PlanOpts pod = po;
+    int w_req = 0;
+    for (uint64_t i = 0; i < n_opts; ++i)
+      if ((long long)opt_lengths[i] == distinct[d]) {
+        const gfft_plan_opts& o = opts[i];
+        if (o.max_pass_len > 0) pod.max_pass_len = o.max_pass_len;
+        pod.radix_order = o.radix_order;
+        if (o.max_radix) pod.max_radix = o.max_radix;
+        w_req = o.units_per_block;
+        break;
+      }
     HostPlan hp;
-    if (gfft_plan_build(hp, distinct[d], 1, r->dbl, trans_id, 1, po) != 0 || hp.nglobal > 3) {
+    if (gfft_plan_build(hp, distinct[d], 1, r->dbl, trans_id, 1, pod) != 0 || hp.nglobal > 3) {
       free_ragged(r);
       return GFFT_E_INVALID_SIZE;
     }
@@ -330,14 +357,19 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
       for (int i = 0; i < gp.npass; ++i) rp.pass[g][i] = gp.pass[i];
       if (hp.nglobal == 1) {
         // groups of whole transforms: about 4096 (FP32) / 2048 (FP64) points
-        int W = std::max<int>(1, (r->dbl ? 2048 : 4096) / gp.L);
+        int W = w_req > 0 ? w_req : std::max<int>(1, (r->dbl ? 2048 : 4096) / gp.L);
         while (W > 1 && 2LL * W * engine_padded(gp.L, r->dbl) * esz > po.smem_budget) --W;
         rp.W[g] = W;
       } else {
-        // columns per item: a power of two, about TILE points, within the transform
+        // columns per item: a power of two, about TILE points (or the
+        // requested count), within the transform and the shared-memory budget
         const long long stride = distinct[d] / gp.L;
         long long W = 1;
-        while (2 * W * gp.L <= TILE && 2 * W <= stride && 2 * W <= 256) W *= 2;
+        if (w_req > 0)
+          while (2 * W <= w_req && 2 * W <= stride && 2 * 2 * W * engine_padded(gp.L, r->dbl) * esz <= po.smem_budget)
+            W *= 2;
+        else
+          while (2 * W * gp.L <= TILE && 2 * W <= stride && 2 * W <= 256) W *= 2;
         rp.W[g] = (int)W;
         rp.tiles[g] = (int)((stride + W - 1) / W);
       }
@@ -353,6 +385,7 @@ int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* siz
   }
   r->nplans = (int)plans.size();
   r->lanes_max = lanes_max;
+  r->hplans = plans;
   // work items, largest first
   std::vector<std::vector<long long>> members(distinct.size());
   for (uint64_t i = 0; i < count; ++i) {
@@ -580,6 +613,31 @@ int gfft_ragged_get_info(gfft_ragged* r, uint64_t* total_points, uint64_t* items
   if (max_passes) *max_passes = r->max_passes;
   if (grid) *grid = r->grid;
   return GFFT_OK;
+}
+
+int gfft_ragged_get_plan(gfft_ragged* r, uint64_t n, gfft_plan_info* info) {
+  if (!r || r->magic != 0x6A66ED00u) return GFFT_E_INVALID_HANDLE;
+  if (!info) return GFFT_E_NULL_POINTER;
+  for (const RaggedPlan& p : r->hplans) {
+    if ((uint64_t)p.n != n) continue;
+    std::memset(info, 0, sizeof(*info));
+    info->n = n;
+    info->batch = 0;
+    info->vtype_id = r->dbl ? 0 : 1;
+    info->trans_id = r->inverse ? 1 : 0;
+    info->place_id = 1;
+    info->n_global_passes = p.nglobal;
+    for (int g = 0; g < p.nglobal && g < 4; ++g) {
+      info->pass_len[g] = p.L[g];
+      for (int i = 0; i < p.npass[g] && i < 15; ++i) info->radices[g][i] = p.pass[g][i].R;
+      info->threads[g] = (int)r->threads;
+      info->units[g] = p.W[g];
+      info->kernel_variant[g] = 1;  // the run-time engine passes (or a compiled shape of them)
+    }
+    info->kernels_per_exec = 1;
+    return GFFT_OK;
+  }
+  return GFFT_E_INVALID_SIZE;
 }
 
 int gfft_ragged_get_status(gfft_ragged* r, int* status) {

@@ -99,6 +99,8 @@ struct EngineArgs {
   const long long* lane_off;  // mode 2: element offset of each lane's transform
   int ldcg;           // read the input through L2 only (data written by other blocks of this launch)
   int notw;           // lane passes without the four-step twiddle (axis transforms of a multi-dimensional array)
+  const void* ftw;    // variant 9, later global passes: W_(16 Ns)^(k r) at [r * Ns + k] (null: two-level lookups)
+  int dif;            // generic engine: frequency decimation (transposed passes, twiddles after the butterflies)
   BlockPass pass[GFFT_MAXP];
 };
 
@@ -113,6 +115,7 @@ struct GlobalPass {
   BlockPass pass[GFFT_MAXP];
   size_t smem;
   int stages;     // variant 2: TMA pipeline depth
+  int rf = 0;     // variant 9: real pre (2) / post (1) pass fused into this pass
   long long ntiles;
   int tile_bytes;
 };
@@ -128,6 +131,7 @@ struct PlanOpts {
   // internal (ragged batches): largest single-pass length and shared-memory budget
   int max_single = 0;
   int smem_budget = 0;
+  int dif = 0;  // frequency decimation (generic engine only)
 };
 
 // ---- ragged batches: one persistent launch over transforms of many sizes --
@@ -184,12 +188,14 @@ struct HostPlan {
   int nglobal = 0;
   GlobalPass gp[GFFT_MAXG];
   int real_fused = 0;     // real pre/post pass inside the single global pass
+  int dif = 0;            // frequency decimation: global passes run last to first, transposed
   // host copy of the device tables (FP64 values; converted at upload)
   std::size_t tw_count = 0;      // in-block twiddles (complex)
   std::size_t gtw_lo_off = 0, gtw_hi_off = 0, gtw_B = 1;
   std::size_t rtw_off = 0;
   int cluster = 0;                // variant 8: W_N^j, j < n, at cluster_tw_off
   std::size_t cluster_tw_off = 0;
+  std::size_t ftw_off[GFFT_MAXG] = {0, 0, 0, 0};  // variant-9 four-step factor tables (0: none)
   std::size_t table_count = 0;   // total complex entries
   std::size_t ws_elems = 0;      // workspace, complex elements
   int n_ws = 0;                  // number of workspace buffers (0..2)

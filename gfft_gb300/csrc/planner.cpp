@@ -27,7 +27,7 @@
 
 bool spec_radices(const GlobalPass& gp);
 // fft_col.cu: launch shape of the tensor-copy column tiles (variant 9)
-extern "C" int gfft_col_shape(int dbl, int L, int stages, int* units, int* threads, size_t* smem);
+extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int* units, int* threads, size_t* smem);
 
 namespace {
 
@@ -250,6 +250,9 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   plan.place = place;
   PlanOpts o = opts;
   if (o.max_radix <= 0) o.max_radix = 16;
+  // frequency decimation runs on the generic engine
+  if (o.dif) o.variant = 1;
+  plan.dif = o.dif ? 1 : 0;
 
   const int esz = dbl ? 16 : 8;
   const int pad_shift = dbl ? 3 : 4;
@@ -467,9 +470,12 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     if (col_ok && plan.nglobal > 1 && gp.L >= 64 && gp.L <= col_max && spec_radices(gp)) {
       int W = 0, T = 0;
       size_t sm = 0;
-      int S = o.stages > 0 ? o.stages : 2;
-      if (gfft_col_shape(dbl, gp.L, S, &W, &T, &sm) == 0 && (n / gp.L) % W == 0 && (g == 0 || Ns % W == 0)) {
-        while (S > 1 && sm > 227 * 1024) gfft_col_shape(dbl, gp.L, --S, &W, &T, &sm);
+      // two stages for passes up to 256, one above (measured on GB300: the
+      // larger L1 left by one stage serves the twiddle tables of the longer
+      // in-block pass sequences)
+      int S = o.stages > 0 ? o.stages : (gp.L >= 512 ? 1 : 2);
+      if (gfft_col_shape(dbl, gp.L, S, 0, &W, &T, &sm) == 0 && (n / gp.L) % W == 0 && (g == 0 || Ns % W == 0)) {
+        while (S > 1 && sm > 227 * 1024) gfft_col_shape(dbl, gp.L, --S, 0, &W, &T, &sm);
         if (sm <= 227 * 1024) {
           gp.variant = 9;
           gp.units = W;
@@ -511,6 +517,31 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     plan.rtw_off = off;
     off += (std::size_t)n;
     plan.real_fused = plan.nglobal == 1 ? 1 : 0;
+    // several passes, all tensor-copy column tiles: the real post pass in the
+    // last pass (forward), the pre pass in the first (inverse), where the
+    // pass's real-pair tiles fit the shared memory
+    bool all9 = plan.nglobal > 1;
+    for (int g = 0; g < plan.nglobal; ++g) all9 = all9 && plan.gp[g].variant == 9;
+    if (all9) {
+      GlobalPass& gp = plan.gp[trans == 2 ? plan.nglobal - 1 : 0];
+      const int rf = trans == 2 ? 1 : 2;
+      int W = 0, T = 0;
+      size_t sm = 0;
+      if (gfft_col_shape(dbl, gp.L, gp.stages, rf, &W, &T, &sm) == 0 && sm <= 227 * 1024 && W >= 2 &&
+          (n / gp.L) % W == 0) {
+        gp.rf = rf;
+        gp.smem = sm;
+        plan.real_fused = 1;
+      }
+    }
+  }
+  // variant-9 later passes: W_(16 Ns)^(k r), r < 16, k < Ns, when at most 2^20 entries
+  for (int g = 1; g < plan.nglobal; ++g) {
+    const GlobalPass& gp = plan.gp[g];
+    if (gp.variant == 9 && 16 * gp.Ns <= (1LL << 20)) {
+      plan.ftw_off[g] = off;
+      off += (std::size_t)(16 * gp.Ns);
+    }
   }
   plan.table_count = off;
   // workspace: odd pass counts in place need two buffers
@@ -546,6 +577,15 @@ void gfft_plan_tables(const HostPlan& plan, double* tab) {
   if (plan.trans >= 2)
     for (long long q = 0; q < plan.n; ++q)
       wroot(q, 2 * plan.n, &tab[2 * (plan.rtw_off + q)], &tab[2 * (plan.rtw_off + q) + 1]);
+  for (int g = 1; g < plan.nglobal; ++g) {
+    if (!plan.ftw_off[g]) continue;
+    const long long ns = plan.gp[g].Ns;
+    for (long long r = 0; r < 16; ++r)
+      for (long long k = 0; k < ns; ++k) {
+        const std::size_t e = plan.ftw_off[g] + (std::size_t)(r * ns + k);
+        wroot(k * r, 16 * ns, &tab[2 * e], &tab[2 * e + 1]);
+      }
+  }
   if (plan.cluster)
     for (long long j = 0; j < plan.n; ++j)
       wroot(j, plan.n, &tab[2 * (plan.cluster_tw_off + j)], &tab[2 * (plan.cluster_tw_off + j) + 1]);

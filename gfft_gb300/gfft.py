@@ -335,19 +335,42 @@ class TransformND(TransformObject):
 class RaggedBatch:
     """Transforms of many lengths (back to back, in the order of ``sizes``)
     in one persistent launch replayed from a CUDA graph (gfft_ragged_*).
-    ``fft(src, dst)`` takes device tensors on the current stream."""
+    ``fft(src, dst)`` takes device tensors on the current stream.
 
-    def __init__(self, sizes, VType=FLOAT, Type=DFT):
+    ``schedule``: None (the planner's defaults), ``{length: plan options}``
+    (gfft_ragged_create_opts: pass split, radix order, units per work item)
+    or ``"tuned"``: the autotuner's measured schedule
+    (``tuner.ragged_schedule``)."""
+
+    def __init__(self, sizes, VType=FLOAT, Type=DFT, schedule=None):
         import numpy as _np
         self.sizes = _np.ascontiguousarray(_np.asarray(sizes, dtype=_np.uint64))
         self.VType, self.Type = VType, Type
+        if isinstance(schedule, str):
+            if schedule != "tuned":
+                raise ValueError("schedule: None, a dict or 'tuned'")
+            from . import tuner
+            schedule = tuner.ragged_schedule(self.sizes, VType.ID, Type.ID)
+        self.schedule = dict(schedule or {})
         L = _lib.lib()
         h = ctypes.c_void_p()
-        st = L.gfft_ragged_create(ctypes.byref(h), int(self.sizes.size),
-                                  self.sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), VType.ID, Type.ID)
-        _lib.check(st, "gfft_ragged_create")
+        lens = _np.ascontiguousarray(_np.array(sorted(self.schedule), dtype=_np.uint64))
+        opts = (_lib.PlanOpts * max(1, len(lens)))()
+        for i, n in enumerate(lens):
+            for k, v in self.schedule[int(n)].items():
+                setattr(opts[i], k, int(v))
+        st = L.gfft_ragged_create_opts(ctypes.byref(h), int(self.sizes.size),
+                                       self.sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), VType.ID, Type.ID,
+                                       int(lens.size), lens.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), opts)
+        _lib.check(st, "gfft_ragged_create_opts")
         self._h = h
         self.total_points = int(self.sizes.sum())
+
+    def plan(self, n):
+        """The schedule used for length n (gfft_ragged_get_plan)."""
+        inf = _lib.PlanInfo()
+        _lib.check(_lib.lib().gfft_ragged_get_plan(self._h, int(n), ctypes.byref(inf)), "gfft_ragged_get_plan")
+        return _lib.info_dict(inf)
 
     def info(self):
         tp, it = ctypes.c_uint64(), ctypes.c_uint64()

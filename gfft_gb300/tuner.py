@@ -8,7 +8,9 @@
   feature normalisation kept beside the weights; ``save`` / ``load`` persist
   both (the tuner's only state, with the timing table);
 - ``choose``: the plan the model ranks first, or the best measured among its
-  top ``k`` (a pruned search; ``k=None`` falls back to the exhaustive one).
+  top ``k`` (a pruned search; ``k=None`` falls back to the exhaustive one);
+- ``ragged_schedule``: the tile / radix schedule of a ragged batch, measured
+  per length inside the ragged kernel itself.
 """
 from __future__ import annotations
 
@@ -236,3 +238,64 @@ def default_plan_ms(row_group):
 
 def gflops(n, batch, ms):
     return 5.0 * n * math.log2(max(n, 2)) * batch / ms / 1e6
+
+
+# schedules a ragged batch may give one length (gfft_ragged_create_opts):
+# radix order, units per work item, pass split
+RAGGED_CANDIDATES = [{}, {"radix_order": 1}, {"radix_order": 2}, {"units_per_block": 2}, {"units_per_block": 8},
+                     {"max_pass_len": 256}, {"max_pass_len": 512}]
+
+
+def time_ragged(n, members, vtype=1, trans=0, opts=None, reps=5):
+    """ms of one ragged launch over `members` transforms of length n with the
+    schedule `opts` for n (None when the schedule cannot be built)."""
+    import torch
+
+    from . import gfft as G
+    try:
+        rb = G.RaggedBatch([n] * members, G.VALUE_TYPES[vtype], G.TRANSFORM_TYPES[trans],
+                           schedule={n: opts} if opts else None)
+    except _lib.GfftError:
+        return None
+    dt = torch.float64 if vtype in (0, 2) else torch.float32
+    x = torch.rand(2 * n * members, device="cuda", dtype=dt)
+    y = torch.empty_like(x)
+    for _ in range(2):
+        rb.fft(x, y)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        rb.fft(x, y)
+    e1.record()
+    torch.cuda.synchronize()
+    rb.close()
+    return e0.elapsed_time(e1) / reps
+
+
+def ragged_schedule(sizes, vtype=1, trans=0, cands=None, coverage=0.9, max_members=64, reps=5, log=None):
+    """The measured schedule of a ragged batch: for the distinct lengths that
+    carry `coverage` of the points (largest share first), every candidate in
+    `cands` (default RAGGED_CANDIDATES) is timed inside the ragged kernel on
+    up to `max_members` transforms of that length; returns {length: opts}
+    for the lengths whose fastest schedule is not the default."""
+    cands = RAGGED_CANDIDATES if cands is None else cands
+    sizes = np.asarray(sizes, dtype=np.int64)
+    lengths, counts = np.unique(sizes, return_counts=True)
+    pts = lengths * counts
+    total = float(pts.sum())
+    chosen, acc = {}, 0.0
+    for idx in np.argsort(-pts, kind="stable"):
+        if acc >= coverage * total:
+            break
+        acc += float(pts[idx])
+        n, m = int(lengths[idx]), int(min(counts[idx], max_members))
+        best = None
+        for c in cands:
+            t = time_ragged(n, m, vtype, trans, c, reps)
+            if t is not None and (best is None or t < best[0]):
+                best = (t, c)
+        if log:
+            log(n, m, best)
+        if best and best[1]:
+            chosen[n] = dict(best[1])
+    return chosen

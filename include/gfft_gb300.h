@@ -100,7 +100,11 @@ typedef struct gfft_plan_opts {
                                  16-byte aligned, others run through variant 5) */
   int stages;             /* bulk-copy pipeline depth of the fast path (0 = 2) */
   int blocks_per_sm;      /* persistent blocks per SM of the fast path (0 = occupancy) */
-  int reserved[4];
+  int decimation;         /* 0 = in time (DIT, default), 1 = in frequency (DIF: the transposed
+                             Stockham passes in reverse order, twiddles after the butterflies;
+                             the reference's InFreq / T_DFTk_x_Im, src/gfftalgfreq.h:106-432);
+                             DIF runs on the generic engine (kernel variant 1) */
+  int reserved[3];
 } gfft_plan_opts;
 
 int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id, int dim,
@@ -219,6 +223,19 @@ int gfft_mlp_destroy(gfft_mlp* m);
 typedef struct gfft_ragged gfft_ragged;
 
 int gfft_ragged_create(gfft_ragged** handle, uint64_t count, const uint64_t* sizes, int vtype_id, int trans_id);
+/* The same with a schedule per length: for each of the n_opts lengths
+ * opt_lengths[i], opts[i] sets its pass split (max_pass_len), in-block radix
+ * order and largest radix, and units per work item (units_per_block: columns
+ * of a multi-pass length, transforms of a single-pass group; a power of two
+ * within the block's shared memory); other lengths keep the defaults.  The
+ * project's autotuner (gfft_gb300.tuner.ragged_schedule) measures candidate
+ * schedules of each length inside this kernel and passes the best here.  No
+ * reference counterpart (the reference runs one object per length). */
+int gfft_ragged_create_opts(gfft_ragged** handle, uint64_t count, const uint64_t* sizes, int vtype_id, int trans_id,
+                            uint64_t n_opts, const uint64_t* opt_lengths, const gfft_plan_opts* opts);
+/* The schedule a ragged handle uses for length n: passes, radices, units
+ * per work item (GFFT_E_INVALID_SIZE when n is not in the batch). */
+int gfft_ragged_get_plan(gfft_ragged* handle, uint64_t n, struct gfft_plan_info* info);
 /* Device pointers; the launch sequence is captured into a CUDA graph on the
  * first call for a (src, dst) pair and replayed afterwards. */
 int gfft_ragged_exec(gfft_ragged* handle, const void* src, void* dst, gfft_stream stream);
@@ -250,8 +267,10 @@ int gfft_ragged_destroy(gfft_ragged* handle);
  * GFFT_E_INVALID_TRANSFORM.
  *
  * The first call on a device looks up the array's address with
- * cudaGetSymbolAddress (the device must be current); make that first call
- * before any stream capture.  All calls share the one array and leave their
+ * cudaGetSymbolAddress (the device must be current).  Under CUDA's lazy
+ * module loading that lookup is also what loads this code onto the device
+ * and reserves the array (about 65 MiB), and it may synchronise the device:
+ * make one warm-up call at start-up, before any stream capture.  All calls share the one array and leave their
  * data in it: nothing needs clearing (each call writes what it reads), but
  * calls that overlap on the GPU -- on two streams, or from two threads
  * without ordering -- race on it and must be serialised by the caller. */

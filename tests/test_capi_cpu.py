@@ -140,10 +140,22 @@ def test_plan_errors():
 
 
 def test_real_plans():
-    d = _lib.plan_query(1 << 19, 0, 2, 0, 16)
-    assert d["real_fused"] == 0 and d["kernels_per_exec"] == d["n_global_passes"] + 1
+    """The real pre/post pass runs inside the transform's own launches: the
+    single pass of a short length, the last (forward) / first (inverse) pass
+    of a multi-pass power-of-two length on the tensor-copy column tiles
+    (C2b: FP64 N_real = 2^20 in two launches).  A pass whose real-pair tiles
+    do not fit the shared memory (FP32 passes of 2048) keeps the separate
+    pass; so do plans on other kernels."""
+    for tr in (2, 3):
+        d = _lib.plan_query(1 << 19, 0, tr, 0, 16)
+        assert d["real_fused"] == 1 and d["kernels_per_exec"] == d["n_global_passes"] == 2, d
+        assert d["kernel_variant"] == [9, 9]
     d = _lib.plan_query(2048, 0, 2, 0, 16)
     assert d["real_fused"] == 1 and d["kernels_per_exec"] == 1
+    d = _lib.plan_query(1 << 21, 1, 3, 1, 1)  # first pass 2048 FP32
+    assert d["real_fused"] == 0 and d["kernels_per_exec"] == d["n_global_passes"] + 1, d
+    d = _lib.plan_query(1 << 19, 0, 2, 0, 16, {"kernel_variant": 5})
+    assert d["real_fused"] == 0 and d["kernels_per_exec"] == d["n_global_passes"] + 1, d
 
 
 def test_tags_and_ids():
@@ -244,3 +256,15 @@ def test_compiled_shapes_are_planner_shapes():
         for r in rs:
             L *= r
         assert _lib.plan_query(L, 1, 0, 1, 16)["kernel_variant"] == [7], rs
+
+
+def test_decimation_option():
+    """decimation = 1 (frequency decimation) plans every pass on the generic
+    engine; other values, or another kernel variant with it, are rejected."""
+    for n, vt in ((64, 0), (1000, 1), (1 << 20, 1), (3 * 2 ** 14, 0)):
+        d = _lib.plan_query(n, vt, 0, 1, 1, {"decimation": 1})
+        assert set(d["kernel_variant"]) == {1}, d
+    for bad in ({"decimation": 2}, {"decimation": -1}, {"decimation": 1, "kernel_variant": 9}):
+        with pytest.raises(_lib.GfftError) as e:
+            _lib.plan_query(64, 0, 0, 1, 1, bad)
+        assert e.value.status == 14

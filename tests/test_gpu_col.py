@@ -119,19 +119,37 @@ def test_col_unaligned_buffers(cuda, n):
     assert np.array_equal(b, b2)
 
 
-@pytest.mark.parametrize("n,dbl", [(1 << 19, 1), (1 << 16, 0), (1 << 21, 0)])
-def test_col_real_transforms(cuda, n, dbl):
-    """Real transforms whose complex half-length runs through variant 9:
-    forward against numpy's FP64 real DFT in the packed layout (X_0, X_n,
-    X_1 .. X_{n-1}) and the inverse round trip."""
+REAL = [(1 << 19, 1, 2, 0), (1 << 19, 1, 3, 1), (1 << 13, 1, 3, 1), (1 << 14, 0, 2, 1), (1 << 16, 0, 2, 0),
+        (1 << 17, 1, 1, 1), (1 << 20, 0, 1, 1), (1 << 21, 0, 1, 1), (1 << 23, 0, 1, 1)]
+
+
+@pytest.mark.parametrize("n,dbl,B,pl", REAL)
+def test_col_real_transforms(cuda, n, dbl, B, pl):
+    """Real transforms of 2n reals whose complex half-length n runs through
+    variant 9, with the real post pass fused into the last pass (RDFT) and
+    the pre pass into the first (IRDFT) where the tiles fit: forward against
+    numpy's FP64 real DFT in the packed layout (X_0, X_n, X_1 .. X_{n-1}),
+    against the unfused plan (column tiles of variant 5 and the separate real
+    pass), and the inverse round trip; in and out of place."""
+    from gfft_gb300 import _lib
     vt = 0 if dbl else 1
     dt = np.float64 if dbl else np.float32
-    x = inputs.uniform(5 + n, 2 * n).astype(dt)
-    y = run(cuda, n, vt, 2, 1, x)
-    f = np.fft.rfft(x.astype(np.float64))
-    want = np.empty(2 * n)
-    want[0], want[1] = f[0].real, f[n].real
-    want[2::2], want[3::2] = f[1:n].real, f[1:n].imag
-    assert rel(y, want) <= tol(2 * n, dbl)
-    z = run(cuda, n, vt, 3, 1, y)
+    for tr in (2, 3):
+        d = _lib.plan_query(n, vt, tr, pl, B)
+        if (n, dbl, tr) != (1 << 21, 0, 3):  # an FP32 first pass of 2048 keeps the separate pre pass
+            assert d["real_fused"] == 1 and d["kernels_per_exec"] == d["n_global_passes"], d
+    x = inputs.uniform(5 + n + B, 2 * n * B).astype(dt)
+    y = run(cuda, n, vt, 2, pl, x, batch=B)
+    for t in range(B):
+        f = np.fft.rfft(x[2 * n * t:2 * n * (t + 1)].astype(np.float64))
+        want = np.empty(2 * n)
+        want[0], want[1] = f[0].real, f[n].real
+        want[2::2], want[3::2] = f[1:n].real, f[1:n].imag
+        got = y[2 * n * t:2 * n * (t + 1)]
+        assert rel(got, want) <= tol(2 * n, dbl), (t, rel(got, want))
+    unf = run(cuda, n, vt, 2, pl, x, batch=B, opts={"kernel_variant": 5})
+    assert rel(y, unf) <= tol(2 * n, dbl)
+    z = run(cuda, n, vt, 3, pl, y, batch=B)
     assert rel(z, x) <= 2 * tol(2 * n, dbl)
+    zu = run(cuda, n, vt, 3, pl, y, batch=B, opts={"kernel_variant": 5})
+    assert rel(z, zu) <= 2 * tol(2 * n, dbl)

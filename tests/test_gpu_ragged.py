@@ -134,3 +134,39 @@ SHAPES = {(15, 12, 2), (15, 10, 2), (15, 15, 2), (16, 5, 5), (16, 15, 2), (12, 9
           (16, 10, 2), (16, 12, 2), (16, 9, 2), (16, 15), (10, 5, 5), (15, 9, 2), (16, 9, 3), (15, 15), (15, 9, 3),
           (15, 10, 4), (9, 9, 6), (16, 12, 3), (9, 9, 3), (10, 10, 2), (15, 12, 3), (16, 10, 4), (15, 12), (15, 10),
           (9, 9, 2), (16, 10), (12, 9, 2), (16, 9)}
+
+
+def test_ragged_schedule_from_tuner(cuda):
+    """The autotuner's ragged schedule (tuner.ragged_schedule: every candidate
+    timed inside the ragged kernel on that length's transforms) is what the
+    handle runs: for every scheduled length, the plan the handle reports
+    reflects the chosen options; explicit schedules give the same kind of
+    change; results stay within the oracle bound."""
+    import torch
+    from gfft_gb300 import gfft as G
+    from gfft_gb300 import tuner
+    sizes = np.concatenate([inputs.ragged_sizes(91, 60, 8, 12), [3 * 2 ** 14] * 6, [5 ** 7] * 4, [2 ** 16] * 5])
+    sched = tuner.ragged_schedule(sizes, 1, 0, coverage=0.8, max_members=8, reps=3)
+    rb = G.RaggedBatch(sizes, G.FLOAT, G.DFT, schedule=sched)
+    assert rb.schedule == sched
+    for n, opts in sched.items():
+        p = rb.plan(n)
+        alone = G.RaggedBatch([n], G.FLOAT, G.DFT, schedule={n: opts})
+        assert alone.plan(n) == p, (n, opts, p)  # the tuned schedule, as measured
+        if "max_pass_len" in opts:
+            assert max(p["pass_len"]) <= opts["max_pass_len"], (n, p)
+        if "units_per_block" in opts:
+            assert all(u <= opts["units_per_block"] for u in p["units"]), (n, p)
+    # explicit schedules change what the handle reports
+    big = 3 * 2 ** 14
+    r2 = G.RaggedBatch(sizes, G.FLOAT, G.DFT, schedule={big: {"max_pass_len": 128, "units_per_block": 2}})
+    p2 = r2.plan(big)
+    assert max(p2["pass_len"]) <= 128 and p2["n_global_passes"] >= 3 and max(p2["units"]) <= 2, p2
+    total = int(sizes.sum())
+    x = torch.from_numpy(inputs.uniform(9, 2 * total)).float().cuda()
+    for h in (rb, r2):
+        y = torch.empty_like(x)
+        h.fft(x, y)
+        torch.cuda.synchronize()
+        _check(y.cpu().numpy(), x.cpu().numpy(), sizes, 1, 0)
+        assert h.status() == 0
