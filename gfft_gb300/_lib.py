@@ -28,7 +28,7 @@ EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_create_nd", "gfft_exec", "g
             "gfft_plan_features", "gfft_mlp_create", "gfft_mlp_num_params", "gfft_mlp_get_params", "gfft_mlp_set_params",
             "gfft_mlp_train", "gfft_mlp_predict", "gfft_mlp_gradients", "gfft_mlp_destroy", "gfft_version",
             "gfft_measure_fma_peak"]
-NFEAT = 24
+NFEAT = 25
 
 
 class PlanOpts(ctypes.Structure):

@@ -61,6 +61,7 @@
 #include <stdint.h>
 
 #include "butterflies.cuh"
+#include "colshape.h"
 #include "plan.h"
 #include "spec.cuh"
 #include "tma.cuh"
@@ -73,35 +74,18 @@ using spec::ns_of;
 using spec::radix_of;
 
 template <typename T> constexpr int esz() { return (int)sizeof(typename Vec<T>::t); }
-// units per tile: tiles of about 64 KB, rows of at least 2 units
-template <typename T, int L> constexpr int lanes() {
-  return (65536 / esz<T>()) / L > 64 ? 64 : ((65536 / esz<T>()) / L < 2 ? 2 : (65536 / esz<T>()) / L);
-}
-// Lane stride of the padded work buffer (elements).  In-lane positions are
-// padded by spec::padi (one slot per 2^PS).  Shared memory serves an 8-byte
-// request per half-warp (16 threads, 16 slots of 8 bytes) and a 16-byte one
-// per quarter-warp (8 slots).  The first pass writes with the lane-fastest
-// mapping: a half-warp covers W lanes and 16 / W butterflies whose 16
-// outputs are consecutive, i.e. slots (lane * Lp + j + r) mod 16, so
-// Lp = 16 / W mod 16 spreads them over all 16 slots (W <= 16); for W >= 16
-// and for 16-byte elements an odd Lp does the same.  The later passes keep a
-// lane's butterflies in consecutive threads and do not depend on Lp.
-template <typename T, int L, int W> constexpr int lane_stride() {
-  constexpr int base = L + (L >> spec::Cfg<T>::PS);
-  if (esz<T>() == 16 || W >= 16) return (base & 1) ? base : base + 1;
-  constexpr int want = (16 / W) % 16;
-  return base + ((want - base % 16) + 16) % 16;
-}
+
+// launch shape of a pass (colshape.h: the same arithmetic on the host)
 template <typename T, int L> struct Shape {
   typedef typename Vec<T>::t V;
-  static constexpr int W = lanes<T, L>();
+  static constexpr int W = colshape::lanes(esz<T>(), L);
   static constexpr int NT = W * L / 16;
   static constexpr int NP = npass_of(L);
-  static constexpr int LP = lane_stride<T, L, W>();
+  static constexpr int LP = colshape::lane_stride(esz<T>(), L, W);
   static constexpr int TB = W * L * esz<T>();       // bytes of one tile
   static constexpr int BR = L < 256 ? L : 256;      // rows per tensor box
   static constexpr int NBOX = L / BR;
-  static constexpr int WORK = ((W * LP * esz<T>() + 1023) / 1024) * 1024;
+  static constexpr int WORK = colshape::work_bytes(esz<T>(), L);
 };
 
 // Tile geometry of a pass: RF = 0 one box of W columns; RF = 1, 2 (real
@@ -111,14 +95,13 @@ template <typename T, int L, int RF> struct Geo {
   static constexpr int W = Shape<T, L>::W;
   static constexpr int H = W / 2;
   static constexpr bool F64 = esz<T>() == 16;
-  static constexpr int WA = RF ? H : W;
-  static constexpr int HB = RF ? (F64 ? H : H + 2) : 0;
+  static constexpr int WA = colshape::width_a(esz<T>(), L, RF);
+  static constexpr int HB = colshape::width_b(esz<T>(), L, RF);
   static constexpr int BOFF = F64 ? 0 : 1;  // first needed column inside region B
-  static constexpr int HC = RF ? (F64 ? 1 : 2) : 0;
+  static constexpr int HC = colshape::width_c(esz<T>(), RF);
   static constexpr int OFF_B = WA * L, OFF_C = (WA + HB) * L;  // elements
-  static constexpr int TB = (WA + HB + HC) * L * esz<T>();
-  static constexpr int WORK = Shape<T, L>::WORK > ((TB + 1023) / 1024) * 1024 ? Shape<T, L>::WORK
-                                                                              : ((TB + 1023) / 1024) * 1024;
+  static constexpr int TB = colshape::stage_bytes(esz<T>(), L, RF);
+  static constexpr int WORK = colshape::work_bytes_rf(esz<T>(), L, RF);
 };
 
 // where lane `lane` of tile p finds its column: smem element offset of row s

@@ -1,0 +1,18 @@
+// Host side of the column-tile shapes (colshape.h): what the planner asks
+// of a variant-9 pass, without CUDA.
+#include <cstddef>
+
+#include "colshape.h"
+
+// Shape of the variant-9 pass of length L (rf: 0 complex, 1 / 2 real
+// forward post / inverse pre pass): units per tile, threads, and the shared
+// memory of `stages` stages; 1 if L (or the real pass) has no kernel.
+extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int* units, int* threads, size_t* smem) {
+  using namespace gfft::colshape;
+  const int esz = dbl ? 16 : 8;
+  if (!supported(esz, L, rf) || stages < 1 || !units || !threads || !smem) return 1;
+  *units = lanes(esz, L);
+  *threads = gfft::colshape::threads(esz, L);
+  *smem = (size_t)smem_bytes(esz, L, rf, stages);
+  return 0;
+}

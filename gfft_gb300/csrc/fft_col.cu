@@ -12,7 +12,6 @@
 
 // fft_col_real.cu: the kernel of a real pass (rf 1: forward post, 2: inverse pre), null if not compiled
 extern "C" const void* gfft_col_real_fn(int dbl, int L, int rf);
-extern "C" int gfft_col_real_smem(int dbl, int L, int rf, int* tb, int* work);
 
 namespace {
 
@@ -65,53 +64,7 @@ const void* kernel_of(int dbl, int L, int rf) {
   if (rf) return gfft_col_real_fn(dbl, L, rf);
   return dbl ? col_fn<double>(L) : col_fn<float>(L);
 }
-template <typename T>
-void col_shape(int L, int* W, int* NT, int* work) {
-  switch (L) {
-#define GFFT_COL_SHAPE(LL)                                \
-  case LL:                                                \
-    *W = gfft::col::Shape<T, LL>::W;                      \
-    *NT = gfft::col::Shape<T, LL>::NT;                    \
-    *work = gfft::col::Shape<T, LL>::WORK;                \
-    return;
-    GFFT_COL_SHAPE(64)
-    GFFT_COL_SHAPE(128)
-    GFFT_COL_SHAPE(256)
-    GFFT_COL_SHAPE(512)
-    GFFT_COL_SHAPE(1024)
-    GFFT_COL_SHAPE(2048)
-    GFFT_COL_SHAPE(4096)
-#undef GFFT_COL_SHAPE
-    default: *W = *NT = *work = 0;
-  }
-}
-
 }  // namespace
-
-// Shape of the variant-9 pass of length L (rf: 0 complex, 1 / 2 real
-// forward post / inverse pre pass): units per tile, threads, and the shared
-// memory of `stages` stages; 1 if L (or the real pass) has no kernel.
-extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int* units, int* threads, size_t* smem) {
-  int W = 0, NT = 0, work = 0;
-  if (dbl) {
-    if (L > 2048) return 1;
-    col_shape<double>(L, &W, &NT, &work);
-  } else {
-    col_shape<float>(L, &W, &NT, &work);
-  }
-  if (!W) return 1;
-  size_t tb = (size_t)W * L * (dbl ? 16 : 8);
-  if (rf) {
-    int rtb = 0, rwork = 0;
-    if (gfft_col_real_smem(dbl, L, rf, &rtb, &rwork) != 0) return 1;
-    tb = (size_t)rtb;
-    work = rwork;
-  }
-  *units = W;
-  *threads = NT;
-  *smem = (size_t)stages * tb + (size_t)work + 8 * (size_t)stages;
-  return 0;
-}
 
 extern "C" int gfft_col_setup(int dbl, size_t max_smem) {
   if (get_encoder() != 0) return 1;
@@ -141,12 +94,8 @@ extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, unsigned grid, unsi
   const int rf = a->real;
   const void* f = kernel_of(dbl, a->L, rf);
   if (!f || !g_encode) return (int)cudaErrorInvalidValue;
-  int W = 0, NT = 0, work = 0;
-  if (dbl)
-    col_shape<double>(a->L, &W, &NT, &work);
-  else
-    col_shape<float>(a->L, &W, &NT, &work);
   const int esz = dbl ? 16 : 8;
+  const int W = gfft::colshape::lanes(esz, a->L);
   const long long batch = a->nunits / a->stride;
   const int br = a->L < 256 ? a->L : 256;
   if ((((uintptr_t)a->in) | ((uintptr_t)a->out)) & 15) return (int)cudaErrorInvalidValue;

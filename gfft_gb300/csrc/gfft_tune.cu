@@ -52,7 +52,7 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   const int orders[] = {0, 1, 2};
   const int radices[] = {16, 8, 4};
   const int variants[] = {0, 1};
-  const int caps[] = {0, 256, 64};
+  const int caps[] = {0, 4096, 1024, 256, 64};
   struct K {
     int cap, v, mr, ro, st, w;
   };
@@ -65,8 +65,10 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   // wider column tiles (128- and 256-byte rows) with shorter passes
   for (int cap : {0, 512, 256, 128})
     for (int w : {16, 32}) ks.push_back({cap, 0, 16, 0, 0, w});
-  // the prefetching column tiles where the specialised ones are the default
+  // the prefetching and the specialised column tiles where the tensor-copy
+  // ones are the default
   for (int cap : caps) ks.push_back({cap, 4, 16, 0, 0, 0});
+  for (int cap : caps) ks.push_back({cap, 5, 16, 0, 0, 0});
   for (int cap : caps)
     for (int v : variants)
       for (int mr : radices)
@@ -90,7 +92,7 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
     if (k.st != 0) {  // a depth variant only where a pipelined kernel runs
       bool pipelined = false;
       for (int g = 0; g < info.n_global_passes; ++g)
-        pipelined |= (info.kernel_variant[g] == 2 || info.kernel_variant[g] == 3);
+        pipelined |= (info.kernel_variant[g] == 2 || info.kernel_variant[g] == 3 || info.kernel_variant[g] == 9);
       if (!pipelined) continue;
     } else {
       bool dup = false;
@@ -171,7 +173,7 @@ int gfft_plan_features(uint64_t n, int vtype_id, int trans_id, int place_id, uin
     lmax = std::max(lmax, info.pass_len[g]);
     lmin = std::min(lmin, info.pass_len[g]);
     const int v = info.kernel_variant[g];
-    f[v <= 1 ? 18 : (v <= 3 ? 19 : (v == 4 ? 20 : 21))] += 1.0f;
+    f[v <= 1 ? 18 : (v <= 3 ? 19 : (v == 4 ? 20 : (v == 9 ? 24 : 21)))] += 1.0f;
   }
   f[15] = (float)(lw / std::max(1, info.n_global_passes));  // mean log2 units (transforms or lanes per block)
   f[16] = (float)std::log2((double)std::max(1, lmax));

@@ -272,12 +272,15 @@ def time_ragged(n, members, vtype=1, trans=0, opts=None, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
-def ragged_schedule(sizes, vtype=1, trans=0, cands=None, coverage=0.9, max_members=64, reps=5, log=None):
+def ragged_schedule(sizes, vtype=1, trans=0, cands=None, coverage=0.9, max_members=512, min_points=1 << 21, reps=5,
+                    margin=0.03, log=None):
     """The measured schedule of a ragged batch: for the distinct lengths that
     carry `coverage` of the points (largest share first), every candidate in
     `cands` (default RAGGED_CANDIDATES) is timed inside the ragged kernel on
-    up to `max_members` transforms of that length; returns {length: opts}
-    for the lengths whose fastest schedule is not the default."""
+    transforms of that length -- as many as the batch holds, raised to at
+    least `min_points` points so that a launch fills the GPU as the whole
+    batch does, at most `max_members`; returns {length: opts} for the
+    lengths whose fastest schedule beats the default by more than `margin`."""
     cands = RAGGED_CANDIDATES if cands is None else cands
     sizes = np.asarray(sizes, dtype=np.int64)
     lengths, counts = np.unique(sizes, return_counts=True)
@@ -288,14 +291,19 @@ def ragged_schedule(sizes, vtype=1, trans=0, cands=None, coverage=0.9, max_membe
         if acc >= coverage * total:
             break
         acc += float(pts[idx])
-        n, m = int(lengths[idx]), int(min(counts[idx], max_members))
-        best = None
+        n = int(lengths[idx])
+        m = int(min(max(counts[idx], -(-min_points // n)), max_members))
+        best, t_default = None, None
         for c in cands:
             t = time_ragged(n, m, vtype, trans, c, reps)
-            if t is not None and (best is None or t < best[0]):
+            if t is None:
+                continue
+            if not c:
+                t_default = t
+            if best is None or t < best[0]:
                 best = (t, c)
         if log:
-            log(n, m, best)
-        if best and best[1]:
+            log(n, m, best, t_default)
+        if best and best[1] and (t_default is None or best[0] < (1.0 - margin) * t_default):
             chosen[n] = dict(best[1])
     return chosen

@@ -181,7 +181,7 @@ int gfft_selftest_bounded_wait(long long spin_limit, int* status);
  * through gfft_plan_opts; gfft_tune_measure times each on caller-provided
  * device buffers (exhaustive measured search, `reps` launches each after one
  * warm-up); failed candidates get -1. */
-#define GFFT_NFEAT 24
+#define GFFT_NFEAT 25
 int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
                          gfft_plan_opts* cands, int max_cands, int* ncands);
 int gfft_tune_measure(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
@@ -192,8 +192,10 @@ int gfft_tune_measure(uint64_t n, int vtype_id, int trans_id, int place_id, uint
  * global passes, [8-14] counts of in-block radices 16/8/4/2/3/5/7, [15] mean
  * log2 units per block, [16] log2 longest and [17] shortest pass length,
  * [18-21] passes run by the generic engine / the pipelined single-pass
- * kernels / the prefetching column tiles / the specialised column tiles,
- * [22] pipeline stages requested, [23] first radix / 16.  No GPU needed. */
+ * kernels / the prefetching column tiles / the specialised column tiles
+ * (variants 5-8), [22] pipeline stages requested, [23] first radix / 16,
+ * [24] passes run by the tensor-copy column tiles (variant 9).  No GPU
+ * needed. */
 int gfft_plan_features(uint64_t n, int vtype_id, int trans_id, int place_id, uint64_t batch,
                        const gfft_plan_opts* opts, float* features);
 
