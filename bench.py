@@ -704,6 +704,40 @@ def main():
             "traffic": NCU_TRAFFIC_BYTES.get((n, batch)), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": launch_ms}
 
+    # the split-precision tensor-core form on the same workload: time per
+    # step and relative L2 error of sampled transforms (numpy FP64 FFT) beside
+    # the plain FP32 path's -- the metric's "TC-split vs plain FP32 at equal
+    # error"; no form can beat the plain one by more than 1 / roofline.frac here
+    tc = None
+    if world == 1:
+        import numpy as np
+        obj_tc = G.TransformObject(n, G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, batch, {"kernel_variant": 6})
+        y_tc = torch.empty_like(x)
+        for _ in range(3):
+            obj_tc.fft(x, y_tc)
+        torch.cuda.synchronize(dev)
+        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0e.record(stream)
+        for _ in range(args.steps):
+            obj_tc.fft(x, y_tc)
+        t1e.record(stream)
+        torch.cuda.synchronize(dev)
+        tc_ms = t0e.elapsed_time(t1e) / args.steps
+        errs = {"tc": [], "plain": []}
+        for tt in (0, batch // 2, batch - 1):
+            xs = x[2 * n * tt:2 * n * (tt + 1)].double().cpu().numpy()
+            ref = np.fft.fft(xs[0::2] + 1j * xs[1::2])
+            for key, yy in (("tc", y_tc), ("plain", y)):
+                ys = yy[2 * n * tt:2 * n * (tt + 1)].double().cpu().numpy()
+                errs[key].append(float(np.linalg.norm((ys[0::2] + 1j * ys[1::2]) - ref) / np.linalg.norm(ref)))
+        tc = {"ms_per_step": tc_ms, "value": flops(n, batch) / (tc_ms * 1e-3) / 1e9, "unit": "GFLOP/s",
+              "speedup_vs_plain": ms / tc_ms, "rel_l2": max(errs["tc"]), "rel_l2_plain": max(errs["plain"]),
+              "bar_rel_l2": 1e-6, "ceiling_vs_plain": 1.0 / roof["frac"],
+              "form": "radix-16 sub-DFTs as FP16 hi/lo products (tcgen05.mma kind::f16, FP32 TMEM accumulators), "
+                      "kernel_variant 6"}
+        obj_tc.close()
+        del y_tc
+
     # end to end through the C ABI host entry point, pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -754,7 +788,7 @@ def main():
                            "plan": {"passes": info["n_global_passes"], "radices": info["radices"],
                                     "threads": info["threads"], "units": info["units"],
                                     "variant": info["kernel_variant"]}},
-                "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+                "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "tc_split": tc,
                 "gpu_launches": args.steps * info["kernels_per_exec"]}
         print(json.dumps(line))
     if world > 1:

@@ -43,9 +43,6 @@ extern "C" int gfft_mixed_setup(int dbl, size_t max_smem);
 extern "C" int gfft_mixed_occupancy(int dbl, const EngineArgs* a, int threads, size_t smem);
 extern "C" int gfft_mixed_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                  cudaStream_t stream);
-extern "C" int gfft_cluster_setup(int dbl, size_t max_smem);
-extern "C" int gfft_cluster_launch(int dbl, const EngineArgs* a, int C, long long batch, unsigned threads, size_t smem,
-                                   cudaStream_t stream);
 extern "C" int gfft_tc_setup(size_t max_smem);
 extern "C" int gfft_tc_occupancy(int L, int threads, size_t smem);
 extern "C" int gfft_tc_launch(const EngineArgs* a, unsigned grid, unsigned threads, size_t smem, cudaStream_t stream);
@@ -79,7 +76,6 @@ int setup_device_once(int dbl) {
   if (gfft_lanep2_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (!dbl && gfft_tc_setup((size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_mixed_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
-  if (gfft_cluster_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_col_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (dev < 64) done[dbl][dev] = true;
   return GFFT_OK;
@@ -175,7 +171,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
     for (int g = 0; g < h->hp.nglobal; ++g) {
       const GlobalPass& gp = h->hp.gp[g];
-      if (gp.variant < 2 || gp.variant == 8) continue;  // 8: one cluster per transform, no persistent grid
+      if (gp.variant < 2) continue;
       int per = (opts && opts->blocks_per_sm)
                     ? opts->blocks_per_sm
                     : (gp.variant == 3   ? gfft_spec_occupancy(dbl, gp.L, gp.threads, gp.smem)
@@ -395,12 +391,6 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
     a.conj = inverse ? 1 : 0;
     a.scale = (inverse && last) ? 1.0 / (double)n : 1.0;
     a.status = h->d_status;
-    if (gp.variant == 8) {
-      a.gtw_lo = tab + p.cluster_tw_off * esz;  // W_N^j
-      if (gfft_cluster_launch(dbl, &a, gp.units, batch, (unsigned)gp.threads, gp.smem, stream) != 0)
-        return GFFT_E_CUDA;
-      continue;
-    }
     if (gp.variant == 6) {
       a.ntiles = gp.ntiles;
       a.spin_limit = 1LL << 26;

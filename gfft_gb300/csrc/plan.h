@@ -193,8 +193,6 @@ struct HostPlan {
   std::size_t tw_count = 0;      // in-block twiddles (complex)
   std::size_t gtw_lo_off = 0, gtw_hi_off = 0, gtw_B = 1;
   std::size_t rtw_off = 0;
-  int cluster = 0;                // variant 8: W_N^j, j < n, at cluster_tw_off
-  std::size_t cluster_tw_off = 0;
   std::size_t ftw_off[GFFT_MAXG] = {0, 0, 0, 0};  // variant-9 four-step factor tables (0: none)
   std::size_t table_count = 0;   // total complex entries
   std::size_t ws_elems = 0;      // workspace, complex elements

@@ -259,35 +259,6 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   const long long smem_budget = o.smem_budget > 0 ? o.smem_budget : 160 * 1024;
   auto padded = [&](long long L) { return L + (L >> pad_shift) + 1; };  // spec / fast kernels
   auto epadded = [&](long long L) { return engine_padded(L, dbl); };     // run-time engine kernels
-  // one transform per thread-block cluster (fft_cluster.cu, variant 8), on
-  // request: N = C x M, M = one tile (4096 FP32 / 2048 FP64), C = 2, 4 or 8;
-  // the passes of the length-M plan, then W_N^j for the cross-CTA step.
-  // Slower than the default plans on GB300 (1.2x - 2.5x the time), so not
-  // chosen by default.
-  {
-    const long long Mcl = dbl ? 2048 : 4096;
-    const bool fits = n == 2 * Mcl || n == 4 * Mcl || n == 8 * Mcl;
-    if (fits && trans < 2 && o.variant == 8 && o.threads == 0 && o.units == 0 &&
-        o.radix_order == 0 && o.max_radix == 16 && o.max_pass_len == 0 && o.max_single == 0) {
-      HostPlan sub;
-      PlanOpts so;
-      if (gfft_plan_build(sub, Mcl, batch, dbl, 0, 1, so) != 0 || sub.nglobal != 1) return 1;
-      plan.nglobal = 1;
-      plan.gp[0] = sub.gp[0];
-      GlobalPass& gp = plan.gp[0];
-      gp.mode = 0;
-      gp.variant = 8;
-      gp.units = (int)(n / Mcl);  // CTAs per cluster
-      gp.threads = (int)(Mcl / 16);
-      gp.smem = (size_t)((Mcl + padded(Mcl)) * esz);  // the chunk and the padded work buffer
-      gp.ntiles = batch;
-      plan.tw_count = sub.tw_count;
-      plan.cluster = 1;
-      plan.cluster_tw_off = sub.table_count;
-      plan.table_count = sub.table_count + (std::size_t)n;
-      return 0;
-    }
-  }
   // largest single-pass length: two padded buffers of one transform
   long long cap1 = dbl ? 4096 : 8192;
   if (o.max_pass_len > 0) cap1 = std::min<long long>(cap1, o.max_pass_len);
@@ -586,7 +557,4 @@ void gfft_plan_tables(const HostPlan& plan, double* tab) {
         wroot(k * r, 16 * ns, &tab[2 * e], &tab[2 * e + 1]);
       }
   }
-  if (plan.cluster)
-    for (long long j = 0; j < plan.n; ++j)
-      wroot(j, plan.n, &tab[2 * (plan.cluster_tw_off + j)], &tab[2 * (plan.cluster_tw_off + j) + 1]);
 }

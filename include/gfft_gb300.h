@@ -93,8 +93,6 @@ typedef struct gfft_plan_opts {
                                  passes of 64..4096: radix-16 sub-DFTs as FP16 hi/lo matrix
                                  products accumulated in FP32; used only when requested),
                              7 = column tiles specialised for a mixed-radix pass shape,
-                             8 = one transform per thread-block cluster (N = 2, 4, 8 tiles;
-                                 used only when requested),
                              9 = column tiles moved by 2-D tensor copies (passes of 64..4096
                                  of a multi-pass power-of-two length; device buffers
                                  16-byte aligned, others run through variant 5) */
@@ -148,7 +146,7 @@ typedef struct gfft_plan_info {
   int threads[4], units[4];    /* launch shape of each pass */
   int kernel_variant[4];       /* 1 generic engine, 2 register-resident fast path, 3 specialised,
                                   4 column tiles, 5 specialised column tiles, 6 tensor-core split,
-                                  7 specialised mixed-radix column tiles, 8 cluster,
+                                  7 specialised mixed-radix column tiles,
                                   9 column tiles moved by 2-D tensor copies */
   uint64_t workspace_bytes;    /* device scratch owned by the handle */
   uint64_t table_bytes;        /* device twiddle tables owned by the handle */

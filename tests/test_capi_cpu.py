@@ -61,8 +61,6 @@ def test_plan_shapes(n, vt, passes):
             p *= r
         assert p == L
         prod *= L
-    if d["kernel_variant"] == [8]:  # one cluster of `units` CTAs, each a length-L chunk
-        prod *= d["units"][0]
     assert prod == n
     if passes > 1:
         assert d["workspace_bytes"] == n * (16 if vt in (0, 2) else 8)

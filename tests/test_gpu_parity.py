@@ -445,30 +445,6 @@ def test_cpp_facade_on_gpu(cuda):
 
 
 @pytest.mark.parametrize("dbl", [0, 1])
-@pytest.mark.parametrize("C", [2, 4, 8])
-def test_cluster_kernel(cuda, oracle, C, dbl):
-    """One transform per thread-block cluster (variant 8 on request, N = C tiles):
-    forward and inverse against the exact oracle and the generic engine, in
-    place equal to out of place."""
-    from gfft_gb300 import _lib
-    n = C * (2048 if dbl else 4096)
-    vt = 0 if dbl else 1
-    dt = np.float64 if dbl else np.float32
-    B = 3
-    K8 = {"kernel_variant": 8}
-    assert _lib.plan_query(n, vt, 0, 1, B, K8)["kernel_variant"] == [8]
-    x = inputs.gaussian(41 + n, 2 * n * B).astype(dt)
-    for tr, sign in ((0, 1), (1, -1)):
-        y = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts=K8)
-        ex = oracle.fft_ld(x.astype(np.float64), n, B, sign)
-        assert rel(y, ex) <= tol(n, dbl), (n, tr, rel(y, ex))
-        gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
-        assert rel(y, gen) <= tol(n, dbl), (n, tr, rel(y, gen))
-        yi = run_gpu(cuda, n, vt, tr, 0, x, batch=B, opts=K8)
-        assert np.array_equal(y, yi), (n, tr)
-
-
-@pytest.mark.parametrize("dbl", [0, 1])
 @pytest.mark.parametrize("n,B", [(768, 7), (625, 5), (576, 3), (432, 9), (1000, 3), (729, 2), (480, 5), (360, 11),
                                  (3 * 2 ** 18, 2), (5 ** 8, 2), (2 ** 10 * 3 ** 5, 3), (1000 * 1000, 1)])
 def test_mixed_columns(cuda, oracle, n, B, dbl):

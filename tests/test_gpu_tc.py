@@ -90,3 +90,32 @@ def test_tc_split_is_deterministic_and_distinct(cuda):
     p = run(cuda, n, 0, 1, x, batch)
     assert np.array_equal(a, b)
     assert not np.array_equal(a, p)
+
+
+def test_tc_split_full_c3_config(cuda, oracle):
+    """The precision configuration at full size: 65536 FP32 transforms of
+    4096 points (2 GiB), Gaussian plus the 1e-4 tone mix, through the split
+    form.  Sampled transforms against the long-double oracle at the 1e-6 bar,
+    the plain FP32 path's error beside them on the same transforms, and the
+    whole batch's Parseval ratio (sum |X|^2 / (N sum |x|^2) = 1)."""
+    import torch
+    from gfft_gb300 import gfft as G
+    n, batch = 4096, 65536
+    xt = torch.from_numpy(inputs.gaussian(0x5EED0003, 2 * n * batch, dtype=np.float32)).cuda()
+    tone = torch.from_numpy(inputs.tone_mix(0x5EED0003, n, 1)).cuda()  # the same tones in every transform
+    xt.view(batch, 2 * n).add_(tone.float())
+    y = torch.empty_like(xt)
+    G.TransformObject(n, G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, batch, TC).fft(xt, y)
+    yp = torch.empty_like(xt)
+    G.TransformObject(n, G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, batch).fft(xt, yp)
+    torch.cuda.synchronize()
+    for t in (0, 1, 4097, 33333, batch - 1):
+        s = slice(2 * n * t, 2 * n * (t + 1))
+        xs = xt[s].double().cpu().numpy()
+        ex = oracle.fft_ld(xs, n, 1, 1)
+        e_tc = rel(y[s].cpu().numpy(), ex)
+        e_pl = rel(yp[s].cpu().numpy(), ex)
+        assert e_tc <= TOL_TC, (t, e_tc, e_pl)
+    ex2 = float(torch.sum(xt.double() ** 2))
+    ey2 = float(torch.sum(y.double() ** 2))
+    assert abs(ey2 / (n * ex2) - 1) <= 1e-5
