@@ -273,9 +273,11 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   // lengths with the default radices; passes of 64 .. 2048 (FP32 up to 4096
   // when max_pass_len asks for it: two passes for 2^23 / 2^24, whose
   // 4096-point pass has rows of only two units)
-  const bool col_ok = (n & (n - 1)) == 0 && n < (1LL << 32) && (o.variant == 0 || o.variant == 9) &&
-                      o.threads == 0 && o.units == 0 && o.radix_order == 0 && o.max_radix == 16 &&
-                      o.max_single == 0 && o.smem_budget == 0;
+  // (power-of-two passes of other lengths too: 3 * 2^18 = 1024 x 768 runs
+  // its 1024-point pass here and its 768-point pass on the mixed-radix tiles)
+  const bool pow2n = (n & (n - 1)) == 0;
+  const bool col_ok = n < (1LL << 32) && (o.variant == 0 || o.variant == 9) && o.threads == 0 && o.units == 0 &&
+                      o.radix_order == 0 && o.max_radix == 16 && o.max_single == 0 && o.smem_budget == 0;
   const long long col_max = dbl ? 2048 : 4096;
   long long col_cap = 2048;
   if (o.max_pass_len > 0) col_cap = std::min<long long>(o.max_pass_len, col_max);
@@ -285,7 +287,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     Ls.push_back(n);
   } else {
     bool ok = false;
-    if (col_ok && col_cap >= 64) {
+    if (col_ok && pow2n && col_cap >= 64) {
       for (int P = 2; P <= GFFT_MAXG && !ok; ++P) ok = split_passes(n, P, col_cap, Ls) && Ls.back() >= 64;
     }
     for (int P = 2; P <= GFFT_MAXG && !ok; ++P) ok = split_passes(n, P, capL, Ls);

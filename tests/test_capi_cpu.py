@@ -108,7 +108,7 @@ def test_plan_column_kernel_selection():
 
 def test_plan_mixed_kernel_selection():
     """Mixed-radix pass shapes with a compile-time kernel take variant 7."""
-    assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8)["kernel_variant"] == [5, 7]
+    assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8)["kernel_variant"] == [9, 7]  # power-of-two pass on variant 9
     assert _lib.plan_query(5 ** 8, 0, 0, 1, 8)["kernel_variant"] == [7, 7]
     assert _lib.plan_query(768, 1, 0, 1, 100)["kernel_variant"] == [7]
     assert _lib.plan_query(768, 1, 0, 1, 100, {"kernel_variant": 1})["kernel_variant"] == [1]
