@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--planner-train", type=int, default=150, help="training sizes (about 13 plans each)")
     p.add_argument("--planner-test", type=int, default=200, help="held-out sizes up to 2^27")
     p.add_argument("--planner-out", default="", help="directory for the timing table and model weights")
+    p.add_argument("--planner-members", type=int, default=5, help="networks in the cost-model ensemble")
+    p.add_argument("--planner-epochs", type=int, default=2000, help="training epochs of each network")
     p.add_argument("--opts", default="", help="with --suite: plan options as JSON, e.g. '{\"kernel_variant\": 1}'")
     p.add_argument("--only", default="", help="with --suite: run the configurations whose name contains this")
     p.add_argument("--dtype", default="f32", choices=["f32", "f64"], help="with --case: FP32 or FP64 complex")
@@ -531,9 +533,9 @@ def run_planner(args):
     X = np.array([r["features"] for r in rows], dtype=np.float32)
     ms = np.array([r["ms"] for r in rows], dtype=np.float32)
     groups = np.array([r["n"] for r in rows])
-    model = tuner.CostModel(seed=7)
+    model = tuner.CostModel(seed=7, members=args.planner_members)
     t0 = time.perf_counter()
-    loss = model.fit(X, ms, epochs=4000, lr=3e-3, groups=groups)
+    loss = model.fit(X, ms, epochs=args.planner_epochs, lr=3e-3, groups=groups)
     t_train = time.perf_counter() - t0
     res = []
     for n in test_sizes:
@@ -558,7 +560,9 @@ def run_planner(args):
     big = [r for r in res if r["n"] == 1 << 27]
     fl = sum(5.0 * r["n"] * math.log2(r["n"]) * r["batch"] for r in res)
     line = {"config": "c5 learned planner, FP32, %d training lengths (%d timed plans), %d held-out lengths "
-                      "in [1024, 2^27]" % (len(train_sizes), len(rows), len(res)),
+                      "in [1024, 2^27]; ensemble of %d networks x %d epochs" % (len(train_sizes), len(rows), len(res),
+                                                                              args.planner_members,
+                                                                              args.planner_epochs),
             "train_rows": len(rows), "collect_s": t_collect, "train_s": t_train, "train_mse_rel_log_ms": loss,
             "regret_model_top1": stats("model_ms"), "regret_pruned_top3": stats("pruned3_ms"),
             "regret_pruned_top5": stats("pruned5_ms"), "regret_default": stats("default_ms"),

@@ -9,7 +9,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libgfft_gb300.so")
+# GFFT_GB300_DEBUG=1 loads the debug build (device-side bounds checks)
+DEBUG = os.environ.get("GFFT_GB300_DEBUG") == "1"
+LIB_PATH = os.path.join(HERE, "libgfft_gb300_debug.so" if DEBUG else "libgfft_gb300.so")
 
 # status codes (include/gfft_gb300.h)
 GFFT_OK = 0
@@ -18,6 +20,7 @@ STATUS_NAMES = {
     4: "GFFT_E_INVALID_PLACE", 5: "GFFT_E_INVALID_DIM", 6: "GFFT_E_INVALID_PARALL", 7: "GFFT_E_NULL_POINTER",
     8: "GFFT_E_MISALIGNED", 9: "GFFT_E_ALLOC", 10: "GFFT_E_CUDA", 11: "GFFT_E_INVALID_HANDLE",
     12: "GFFT_E_NOT_IN_LIST", 13: "GFFT_E_TIMEOUT", 14: "GFFT_E_INVALID_PLAN", 15: "GFFT_E_TOO_LARGE",
+    16: "GFFT_E_BOUNDS",
 }
 
 # every symbol the header declares, checked by the CPU tests
@@ -27,7 +30,7 @@ EXPORTED = ["gfft_create", "gfft_create_opts", "gfft_create_nd", "gfft_exec", "g
             "gfft_ragged_get_status", "gfft_ragged_destroy", "gfft_tune_candidates", "gfft_tune_measure",
             "gfft_plan_features", "gfft_mlp_create", "gfft_mlp_num_params", "gfft_mlp_get_params", "gfft_mlp_set_params",
             "gfft_mlp_train", "gfft_mlp_predict", "gfft_mlp_gradients", "gfft_mlp_destroy", "gfft_version",
-            "gfft_measure_fma_peak"]
+            "gfft_measure_fma_peak", "gfft_debug_build", "gfft_selftest_bounds_check"]
 NFEAT = 25
 
 
@@ -61,7 +64,7 @@ _lib = None
 
 def build(force=False):
     from . import buildlib
-    return buildlib.build(force=force)
+    return buildlib.build(force=force, debug=DEBUG)
 
 
 def lib():
@@ -110,6 +113,8 @@ def lib():
         L.gfft_mlp_destroy.argtypes = [vp]
         dp = ctypes.POINTER(ctypes.c_double)
         L.gfft_measure_fma_peak.argtypes = [ci, ci, dp, dp]
+        L.gfft_debug_build.argtypes = []
+        L.gfft_selftest_bounds_check.argtypes = [ctypes.POINTER(ci), ctypes.POINTER(ci)]
         for name in EXPORTED:
             getattr(L, name).restype = getattr(L, name).restype or ci
         L.gfft_strerror.restype = ctypes.c_char_p

@@ -42,6 +42,12 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+def lib_path(debug: bool = False) -> str:
+    """The release library, or the debug build (-DGFFT_DEBUG: device-side
+    bounds checks that record GFFT_E_BOUNDS instead of accessing memory)."""
+    return os.path.join(HERE, "libgfft_gb300_debug.so") if debug else LIB
+
+
 def _sources():
     out = []
     for f in os.listdir(CSRC):
@@ -52,38 +58,41 @@ def _sources():
     return out
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB):
+def _stale(lib: str) -> bool:
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return any(os.path.getmtime(s) > t for s in _sources())
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and not _stale():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, debug: bool = False) -> str:
+    lib = lib_path(debug)
+    if not force and not _stale(lib):
+        return lib
+    bdir = BUILD + ("_debug" if debug else "")
+    os.makedirs(bdir, exist_ok=True)
     nv = nvcc()
+    dflag = ["-DGFFT_DEBUG"] if debug else []
     jobs, objs = [], []
     for s in CUDA_SOURCES:
-        o = os.path.join(BUILD, s + ".o")
+        o = os.path.join(bdir, s + ".o")
         objs.append(o)
         extra = ["-Xptxas", "-v"] if verbose else []
-        jobs.append([nv, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, s), "-o", o])
+        jobs.append([nv, *NVCC_FLAGS, *dflag, *extra, "-c", os.path.join(CSRC, s), "-o", o])
     for s in CXX_SOURCES:
-        o = os.path.join(BUILD, s + ".o")
+        o = os.path.join(bdir, s + ".o")
         objs.append(o)
-        jobs.append(["g++", *CXX_FLAGS, "-c", os.path.join(CSRC, s), "-o", o])
+        jobs.append(["g++", *CXX_FLAGS, *dflag, "-c", os.path.join(CSRC, s), "-o", o])
     with ThreadPoolExecutor(len(jobs)) as ex:
         logs = list(ex.map(_run, jobs))
     if verbose:
         for lg in logs:
             sys.stdout.write(lg)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     _run([nv, *ARCH, "-shared", "-cudart", "static", *objs, "-o", tmp])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, debug="--debug" in sys.argv))

@@ -73,7 +73,15 @@ void fill_info(const HostPlan& p, int vtype, size_t tab_bytes, size_t ws_bytes, 
 
 extern "C" {
 
-const char* gfft_version(void) { return "gfft_gb300 0.1 (sm_103a)"; }
+const char* gfft_version(void) { return "gfft_gb300 0.2 (sm_103a)"; }
+
+int gfft_debug_build(void) {
+#ifdef GFFT_DEBUG
+  return 1;
+#else
+  return 0;
+#endif
+}
 
 const char* gfft_strerror(int status) {
   switch (status) {
@@ -94,6 +102,7 @@ const char* gfft_strerror(int status) {
     case GFFT_E_TIMEOUT: return "a bounded device wait timed out";
     case GFFT_E_INVALID_PLAN: return "inconsistent plan options";
     case GFFT_E_TOO_LARGE: return "request exceeds the fixed capacity of this entry point";
+    case GFFT_E_BOUNDS: return "a device-side bounds check of the debug build failed (the access was skipped)";
     default: return "unknown status";
   }
 }

@@ -62,6 +62,7 @@
 
 #include "butterflies.cuh"
 #include "colshape.h"
+#include "dcheck.cuh"
 #include "plan.h"
 #include "spec.cuh"
 #include "tma.cuh"
@@ -188,7 +189,7 @@ __device__ __forceinline__ void real_zero(typename Vec<T>::t* p0, int dir) {
 // s and L - 1 - s (items L/2 .. L-1).
 template <typename T, int L, int RF, int NT>
 __device__ __forceinline__ void real_tile(typename Vec<T>::t* buf, long long p, long long S, long long n,
-                                          const typename Vec<T>::t* __restrict__ rtw) {
+                                          const typename Vec<T>::t* __restrict__ rtw, int* status) {
   typedef Geo<T, L, RF> G;
   typedef typename Vec<T>::t V;
   for (int it = threadIdx.x; it < G::H * L; it += NT) {
@@ -217,7 +218,11 @@ __device__ __forceinline__ void real_tile(typename Vec<T>::t* buf, long long p, 
     }
     const LaneSrc A = lane_src<T, L, RF>(la, p, S), B = lane_src<T, L, RF>(lb, p, S);
     const long long q = A.unit + (long long)sa * S;
-    real_pair<T>(buf + A.base + sa * A.width + A.col, buf + B.base + sb * B.width + B.col, q, n - q, rtw, RF);
+    const int ea = A.base + sa * A.width + A.col, eb = B.base + sb * B.width + B.col;
+    if (GFFT_DCHECK(ea >= 0 && eb >= 0 && ea < G::TB / (int)sizeof(V) && eb < G::TB / (int)sizeof(V) && q > 0 &&
+                        q < n,
+                    status))
+      real_pair<T>(buf + ea, buf + eb, q, n - q, rtw, RF);
   }
 }
 
@@ -252,15 +257,19 @@ template <int W, int NT> __device__ __forceinline__ void group_sync() {
 }
 
 template <typename T, int L, int P, bool LF>
-__device__ __forceinline__ void rd(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* buf) {
+__device__ __forceinline__ void rd(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* buf, int* st) {
   typedef Shape<T, L> S;
   constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R;
+  (void)st;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int lane = lane_of<S::W, S::NT, LF>(q), j = j_of<S::W, S::NT, LF>(q);
     const typename Vec<T>::t* s = buf + lane * S::LP;
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[q * R + r] = s[spec::padi<T>(j + r * NB)];
+    for (int r = 0; r < R; ++r) {
+      const int e = lane * S::LP + spec::padi<T>(j + r * NB);
+      if (GFFT_DCHECK(e >= 0 && e < S::W * S::LP, st)) v[q * R + r] = s[spec::padi<T>(j + r * NB)];
+    }
   }
 }
 
@@ -282,9 +291,10 @@ __device__ __forceinline__ void cp(typename Vec<T>::t (&v)[16], const typename V
 }
 
 template <typename T, int L, int P, bool LF>
-__device__ __forceinline__ void wr(const typename Vec<T>::t (&v)[16], typename Vec<T>::t* buf) {
+__device__ __forceinline__ void wr(const typename Vec<T>::t (&v)[16], typename Vec<T>::t* buf, int* st) {
   typedef Shape<T, L> S;
   constexpr int R = radix_of(L, P), Q = 16 / R, NS = ns_of(L, P);
+  (void)st;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int lane = lane_of<S::W, S::NT, LF>(q), j = j_of<S::W, S::NT, LF>(q);
@@ -292,7 +302,10 @@ __device__ __forceinline__ void wr(const typename Vec<T>::t (&v)[16], typename V
     const int base = (j - k) * R + k;
     typename Vec<T>::t* d = buf + lane * S::LP;
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[spec::padi<T>(base + r * NS)] = v[q * R + r];
+    for (int r = 0; r < R; ++r) {
+      const int e = lane * S::LP + spec::padi<T>(base + r * NS);
+      if (GFFT_DCHECK(e >= 0 && e < S::W * S::LP, st)) d[spec::padi<T>(base + r * NS)] = v[q * R + r];
+    }
   }
 }
 
@@ -300,16 +313,16 @@ __device__ __forceinline__ void wr(const typename Vec<T>::t (&v)[16], typename V
 // the caller synchronises after the last write
 template <typename T, int L, int P>
 __device__ __forceinline__ void middle(typename Vec<T>::t (&v)[16], typename Vec<T>::t* work,
-                                       const typename Vec<T>::t* tw, const BlockPass* bp) {
+                                       const typename Vec<T>::t* tw, const BlockPass* bp, int* st) {
   typedef Shape<T, L> S;
   constexpr int NP = npass_of(L);
   if constexpr (P < NP - 1) {
     if constexpr (P > 1) group_sync<S::W, S::NT>();
-    rd<T, L, P, false>(v, work);
+    rd<T, L, P, false>(v, work, st);
     cp<T, L, P, false>(v, tw, bp[P].tw);
     group_sync<S::W, S::NT>();
-    wr<T, L, P, false>(v, work);
-    middle<T, L, P + 1>(v, work, tw, bp);
+    wr<T, L, P, false>(v, work, st);
+    middle<T, L, P + 1>(v, work, tw, bp, st);
   }
 }
 
@@ -424,7 +437,7 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
     V* const st = reinterpret_cast<V*>(smem + (size_t)s * TB);
     if constexpr (RF == 2) {
       // real inverse: recover Z from the packed spectrum before the butterflies
-      real_tile<T, L, RF, NT>(st, p, stride, a.N, rtw);
+      real_tile<T, L, RF, NT>(st, p, stride, a.N, rtw, a.status);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes before the stage's next copy
       __syncthreads();
     }
@@ -435,7 +448,10 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
       const LaneSrc src = lane_src<T, L, RF>(lane, p, stride);
       const V* sp = st + src.base + src.col;
 #pragma unroll
-      for (int r = 0; r < 16; ++r) v[r] = sp[(j + r * NB0) * src.width];
+      for (int r = 0; r < 16; ++r) {
+        const int e = src.base + src.col + (j + r * NB0) * src.width;
+        if (GFFT_DCHECK(e >= 0 && e < TB / (int)sizeof(V), a.status)) v[r] = sp[(j + r * NB0) * src.width];
+      }
       if (conj)
 #pragma unroll
         for (int r = 0; r < 16; ++r) v[r] = cconj(v[r]);
@@ -468,30 +484,31 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
       const long long nt = tile + (long long)S * G;
       if (nt < a.ntiles) issue(nt, s);
     }
-    wr<T, L, 0, true>(v, work);
+    wr<T, L, 0, true>(v, work, a.status);
     __syncthreads();
-    middle<T, L, 1>(v, work, tw, a.pass);
+    middle<T, L, 1>(v, work, tw, a.pass, a.status);
     if (gNs == 1) {
       // first global pass: lane groups, each lane's L outputs contiguous
       if constexpr (NP > 2) group_sync<W, NT>();
-      rd<T, L, NP - 1, false>(v, work);
+      rd<T, L, NP - 1, false>(v, work, a.status);
       cp<T, L, NP - 1, false>(v, tw, a.pass[NP - 1].tw);
       V* o = (V*)a.out + t * a.N;
 #pragma unroll
       for (int q = 0; q < QL; ++q) {
         const int lane = lane_of<W, NT, false>(q), j = j_of<W, NT, false>(q);
-        V* d = o + lane_src<T, L, RF>(lane, p, stride).unit * L + j;
+        const long long e0 = t * a.N + lane_src<T, L, RF>(lane, p, stride).unit * L + j;
+        V* d = (V*)a.out + e0;
 #pragma unroll
         for (int r = 0; r < RL; ++r) {
           V x = v[q * RL + r];
           if (conj) x = cconj(x);
-          d[r * NBL] = cscale(x, sc);
+          if (GFFT_DCHECK(e0 + r * NBL >= 0 && e0 + r * NBL < a.nunits * L, a.status)) d[r * NBL] = cscale(x, sc);
         }
       }
     } else {
       // later global passes: lane-fastest, dense tile in the work buffer, tensor stores
       if constexpr (NP > 2) __syncthreads();
-      rd<T, L, NP - 1, true>(v, work);
+      rd<T, L, NP - 1, true>(v, work, a.status);
       cp<T, L, NP - 1, true>(v, tw, a.pass[NP - 1].tw);
       __syncthreads();
 #pragma unroll
@@ -502,13 +519,14 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
         for (int r = 0; r < RL; ++r) {
           V x = v[q * RL + r];
           if (conj) x = cconj(x);
-          work[dsrc.base + (j + r * NBL) * dsrc.width + dsrc.col] = cscale(x, sc);
+          const int e = dsrc.base + (j + r * NBL) * dsrc.width + dsrc.col;
+          if (GFFT_DCHECK(e >= 0 && e < Gm::WORK / (int)sizeof(V), a.status)) work[e] = cscale(x, sc);
         }
       }
       if constexpr (RF == 1) {
         // real forward: the packed half spectrum from Z, in place
         __syncthreads();
-        real_tile<T, L, RF, NT>(work, p, stride, a.N, rtw);
+        real_tile<T, L, RF, NT>(work, p, stride, a.N, rtw, a.status);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncthreads();
@@ -545,7 +563,8 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
           const int m = e % (Gm::H + 1), srow = e / (Gm::H + 1);
           if (m < Gm::H) {
             const long long col = stride - p * Gm::H - Gm::H + 1 + m;
-            if (!tb_b && col < stride) o[srow * stride + col] = work[Gm::OFF_B + srow * Gm::HB + Gm::BOFF + m];
+            if (!tb_b && col < stride && GFFT_DCHECK(col >= 0 && srow < L, a.status))
+              o[srow * stride + col] = work[Gm::OFF_B + srow * Gm::HB + Gm::BOFF + m];
           } else if (p == 0) {
             o[srow * stride + stride / 2] = work[Gm::OFF_C + srow * Gm::HC];
           }

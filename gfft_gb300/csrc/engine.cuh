@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "butterflies.cuh"
+#include "dcheck.cuh"
 #include "plan.h"
 
 namespace gfft {
@@ -43,6 +44,7 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
     const V* s = src + lane * a.Lp;
     V* d = dst + lane * a.Lp;
     V v[R];
+    if (!GFFT_DCHECK(lane < a.W && pad<T>(j + (R - 1) * nb) < a.Lp, a.status)) continue;
     if (rd_lin) {
       const V* s0 = s + pad<T>(j);
 #pragma unroll
@@ -59,6 +61,7 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
     }
     dft<T, V, R>(v);
     const int base = (j - k) * R + k;
+    if (!GFFT_DCHECK(pad<T>(base + (R - 1) * (int)p.Ns) < a.Lp, a.status)) continue;
     if (wr_lin) {
       V* d0 = d + pad<T>(base);
 #pragma unroll
@@ -90,6 +93,9 @@ __device__ __forceinline__ void block_pass_dif(const typename Vec<T>::t* __restr
     const int j = i - lane * nb;
     const int k = j - (int)fdiv((unsigned)j, p.fd_ns) * p.Ns;
     const int base = (j - k) * R + k;
+    if (!GFFT_DCHECK(lane < a.W && pad<T>(base + (R - 1) * (int)p.Ns) < a.Lp && pad<T>(j + (R - 1) * nb) < a.Lp,
+                     a.status))
+      continue;
     const V* s = src + lane * a.Lp;
     V* d = dst + lane * a.Lp;
     V v[R];
@@ -256,7 +262,7 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int i = i0 + q * step;
-        v[q] = (i < total && i < lim) ? tile[i] : mk<V>(0, 0);
+        v[q] = (i < total && i < lim && GFFT_DCHECK(u0 * L + i < a.nunits * L, a.status)) ? tile[i] : mk<V>(0, 0);
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
@@ -321,7 +327,8 @@ __device__ __forceinline__ void load_tile(const EngineArgs& a, typename Vec<T>::
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int s = s0 + q * sstep;
-        if (s < L) v[q] = a.ldcg ? __ldcg(src + (long long)s * a.stride) : src[(long long)s * a.stride];
+        if (s < L && GFFT_DCHECK(t * a.N + b + (long long)s * a.stride < a.nunits * L, a.status))
+          v[q] = a.ldcg ? __ldcg(src + (long long)s * a.stride) : src[(long long)s * a.stride];
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
@@ -397,7 +404,7 @@ __device__ __forceinline__ void store_tile(const EngineArgs& a, const typename V
       const int s = i - lane * L;
       V v = buf[lane * a.Lp + pad<T>(s)];
       if (a.conj) v = cconj(v);
-      tile[i] = cscale(v, sc);
+      if (GFFT_DCHECK(u0 * L + i < a.nunits * L, a.status)) tile[i] = cscale(v, sc);
     }
   } else if (a.dif) {
     // lane units of a frequency-decimation pass: the four-step twiddle of
@@ -451,7 +458,8 @@ __device__ __forceinline__ void store_tile(const EngineArgs& a, const typename V
     for (int s = threadIdx.x / W; s < L; s += sstep) {
       V v = bl[pad<T>(s)];
       if (a.conj) v = cconj(v);
-      dstp[(long long)s * a.gNs] = cscale(v, sc);
+      if (GFFT_DCHECK(t * a.N + (b - k) * L + k + (long long)s * a.gNs < a.nunits * L, a.status))
+        dstp[(long long)s * a.gNs] = cscale(v, sc);
     }
   }
 }

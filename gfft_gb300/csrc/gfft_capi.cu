@@ -17,6 +17,7 @@
 
 #include "../../include/gfft_gb300.h"
 #include "capi_host.h"
+#include "dcheck.cuh"
 #include "handle.h"
 #include "plan.h"
 
@@ -499,6 +500,39 @@ int gfft_selftest_bounded_wait(long long spin_limit, int* status) {
   cudaFree(buf);
   gfft_destroy(h);
   return st;
+}
+
+#ifdef GFFT_DEBUG
+}  // extern "C"
+namespace {
+// one check that fails, with no access behind it
+__global__ void dcheck_selftest(int* status) { (void)GFFT_DCHECK(threadIdx.x > 1000u, status); }
+}  // namespace
+extern "C" {
+#endif
+
+int gfft_selftest_bounds_check(int* status, int* line) {
+  if (!status || !line) return GFFT_E_NULL_POINTER;
+#ifdef GFFT_DEBUG
+  int* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(int)) != cudaSuccess) return GFFT_E_ALLOC;
+  int st = GFFT_OK;
+  int h[2] = {0, 0};
+  if (cudaMemset(d, 0, 2 * sizeof(int)) != cudaSuccess) st = GFFT_E_CUDA;
+  if (st == GFFT_OK) {
+    dcheck_selftest<<<1, 1>>>(d);
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+      st = GFFT_E_CUDA;
+  }
+  cudaFree(d);
+  *status = h[0];
+  *line = h[1];
+  return st;
+#else
+  *status = 0;
+  *line = 0;
+  return GFFT_E_INVALID_PLAN;
+#endif
 }
 
 int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {

@@ -303,26 +303,30 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     gp.mode = plan.nglobal == 1 ? 0 : 1;
     std::vector<int> rs = block_radices(gp.L, o);
     if ((int)rs.size() > GFFT_MAXP) return 1;
-    gp.npass = (int)rs.size();
-    int bNs = 1;
-    int rmin = 16;
-    for (int i = 0; i < gp.npass; ++i) {
-      BlockPass& bp = gp.pass[i];
-      bp.R = rs[i];
-      bp.Ns = bNs;
-      bp.tw = (int)tw;
-      bp.gen = -1;
-      tw += (std::size_t)(bp.R - 1) * bNs;
-      bNs *= bp.R;
-      rmin = std::min(rmin, bp.R);
-    }
-    for (int i = 0; i < gp.npass; ++i) {
-      BlockPass& bp = gp.pass[i];
-      if (!native_radix(bp.R)) {
-        bp.gen = (int)tw;
-        tw += bp.R;
+    const std::size_t tw0 = tw;  // this pass's twiddles start here
+    // the in-block passes of radix sequence `seq` and their twiddle offsets
+    auto assign = [&](const std::vector<int>& seq) {
+      tw = tw0;
+      gp.npass = (int)seq.size();
+      int bNs = 1;
+      for (int i = 0; i < gp.npass; ++i) {
+        BlockPass& bp = gp.pass[i];
+        bp.R = seq[(std::size_t)i];
+        bp.Ns = bNs;
+        bp.tw = (int)tw;
+        bp.gen = -1;
+        tw += (std::size_t)(bp.R - 1) * bNs;
+        bNs *= bp.R;
       }
-    }
+      for (int i = 0; i < gp.npass; ++i) {
+        BlockPass& bp = gp.pass[i];
+        if (!native_radix(bp.R)) {
+          bp.gen = (int)tw;
+          tw += bp.R;
+        }
+      }
+    };
+    assign(rs);
     if (gp.mode == 0) {
       long long target = dbl ? 2048 : 4096;  // elements per block
       int W = o.units > 0 ? o.units : (int)std::max<long long>(1, target / gp.L);
@@ -341,6 +345,8 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     gp.threads = thr;
     gp.variant = 1;
     gp.smem = (size_t)(2LL * gp.units * epadded(gp.L) * esz);
+    const int eng_units = gp.units, eng_threads = gp.threads;
+    const size_t eng_smem = gp.smem;
     // register-resident TMA-pipelined path: power-of-two single pass whose
     // radices divide 16, 16 values per thread
     bool pow2ok = gp.mode == 0 && trans < 2 && gp.L >= 16 && (gp.L & (gp.L - 1)) == 0 && o.variant != 1;
@@ -458,6 +464,20 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
           gp.ntiles = batch * (n / gp.L) / W;
         }
       }
+    }
+    // FP32 passes left to the prefetching run-time column tiles (no compiled
+    // shape): the generic engine with the radices in reverse order is
+    // faster.  Measured over 150 lengths 256 .. 2^27 (the planner
+    // evaluation): plans of such passes ran 1.25x (two passes) and 1.48x
+    // (three) the best candidate, the engine in reverse order 1.05x / 1.02x.
+    if (gp.variant == 4 && !dbl && o.variant == 0 && o.radix_order == 0 && o.max_radix == 16 && o.units == 0 &&
+        o.threads == 0 && o.stages == 0 && o.max_single == 0) {
+      assign(std::vector<int>(rs.rbegin(), rs.rend()));
+      gp.variant = 1;
+      gp.units = eng_units;
+      gp.threads = eng_threads;
+      gp.smem = eng_smem;
+      gp.ntiles = 0;
     }
     // length-specialised variant: default radix order, L in the compiled set
     bool spec = gp.variant == 2 && (o.variant == 0 || o.variant == 3) && o.units == 0 && o.threads == 0 &&

@@ -187,6 +187,18 @@ def _as_list(x) -> list:
     return [x]
 
 
+def _learned_opts(n, vtype, trans, place, batch, plan):
+    """Plan options from the learned planner (gfft_gb300.tuner)."""
+    from . import tuner
+    if plan not in ("learned", "measured"):
+        raise ValueError("plan: None, 'learned' or 'measured'")
+    model = tuner.default_model()
+    if model is None:
+        raise RuntimeError("no shipped cost model")
+    opts, _ = tuner.choose(model, n, vtype, trans, place, batch, k=1 if plan == "learned" else 5)
+    return opts
+
+
 class TransformObject:
     """A transform object (the reference's ``Transform<...>::Instance``).
 
@@ -194,7 +206,11 @@ class TransformObject:
     asynchronous on the current torch stream for device tensors.
     """
 
-    def __init__(self, n, vtype, trans, dim=1, parall=Serial, place=OUT_OF_PLACE, batch=1, opts=None):
+    def __init__(self, n, vtype, trans, dim=1, parall=Serial, place=OUT_OF_PLACE, batch=1, opts=None, plan=None):
+        """``plan``: None (the planner's rules, or ``opts``), "learned" (the
+        shipped cost model's first choice among the tuner's candidates, no
+        measurement) or "measured" (the best measured of the model's top 5:
+        the pruned search)."""
         self.n = int(n)
         self.VType = vtype
         self.Type = trans
@@ -202,6 +218,8 @@ class TransformObject:
         self.Place = place
         self.batch = int(batch)
         self.dim = int(dim)
+        if plan is not None and not opts:
+            opts = _learned_opts(self.n, vtype.ID, trans.ID, place.ID, self.batch, plan)
         L = _lib.lib()
         h = ctypes.c_void_p()
         if not opts:  # None or {}: the default plan

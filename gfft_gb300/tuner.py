@@ -134,10 +134,16 @@ class CostModel:
     its capacity on the differences between plans rather than on the overall
     scale, and predictions rank the candidates of a length directly."""
 
-    def __init__(self, seed=1):
-        self.net = MLP(seed=seed)
+    def __init__(self, seed=1, members=1):
+        # an ensemble of `members` networks of different initial weights; the
+        # prediction is the mean of their log-times
+        self.nets = [MLP(seed=seed + 1000 * k) for k in range(max(1, members))]
         self.mu = np.zeros(_lib.NFEAT, dtype=np.float32)
         self.sd = np.ones(_lib.NFEAT, dtype=np.float32)
+
+    @property
+    def net(self):
+        return self.nets[0]
 
     @staticmethod
     def relative_log(ms, groups):
@@ -154,20 +160,24 @@ class CostModel:
         self.mu = X.mean(0)
         self.sd = np.where(X.std(0) > 1e-6, X.std(0), 1.0).astype(np.float32)
         y = self.relative_log(ms, groups) if groups is not None else np.log(np.asarray(ms, dtype=np.float32))
-        return self.net.train((X - self.mu) / self.sd, y, epochs, lr)
+        Xs = (X - self.mu) / self.sd
+        return float(np.mean([net.train(Xs, y, epochs, lr) for net in self.nets]))
 
     def predict_ms(self, X):
         X = (np.asarray(X, dtype=np.float32) - self.mu) / self.sd
-        return np.exp(self.net.predict(X))
+        return np.exp(np.mean([net.predict(X) for net in self.nets], axis=0))
 
     def save(self, path):
-        np.savez(path, params=self.net.params(), mu=self.mu, sd=self.sd)
+        np.savez(path, params=np.stack([net.params() for net in self.nets]), mu=self.mu, sd=self.sd)
 
     @classmethod
     def load(cls, path):
         d = np.load(path)
-        m = cls()
-        m.net.set_params(d["params"])
+        p = d["params"]
+        p = p[None, :] if p.ndim == 1 else p
+        m = cls(members=len(p))
+        for net, q in zip(m.nets, p):
+            net.set_params(q)
         m.mu, m.sd = d["mu"], d["sd"]
         return m
 

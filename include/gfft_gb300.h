@@ -66,7 +66,8 @@ enum {
   GFFT_E_NOT_IN_LIST = 12,      /* size/type not generated by the facade's typelist */
   GFFT_E_TIMEOUT = 13,          /* a bounded device wait ran out (persistent kernels) */
   GFFT_E_INVALID_PLAN = 14,     /* a caller-supplied plan option is inconsistent */
-  GFFT_E_TOO_LARGE = 15         /* request exceeds a fixed capacity of the entry point */
+  GFFT_E_TOO_LARGE = 15,        /* request exceeds a fixed capacity of the entry point */
+  GFFT_E_BOUNDS = 16            /* debug build: a device-side bounds check failed (the access was skipped) */
 };
 
 /* Replaces GenerateTransform<...>::CreateTransformObject(n, vtype_id,
@@ -284,6 +285,17 @@ int gfft_exec_noalloc(uint64_t n, int vtype_id, int trans_id, uint64_t batch, co
  * FP32 rate).  No reference counterpart (its harness reports
  * 5 N log2 N / t only, test/gfft_performance.h:67-78). */
 int gfft_measure_fma_peak(int dbl, int iters, double* gflops, double* ms);
+
+/* 1 for the debug build of the library (compiled with -DGFFT_DEBUG: every
+ * checked shared- and global-memory index of the column-tile and engine
+ * kernels is tested before the access; a failing check skips the access and
+ * leaves GFFT_E_BOUNDS, read by gfft_get_device_status), else 0.  No
+ * reference counterpart (its only guards are an assert and a comment). */
+int gfft_debug_build(void);
+/* Debug build: runs one failing check in a one-thread kernel (no memory
+ * access behind it) and returns the status words it left: GFFT_E_BOUNDS and
+ * the source line.  Release build: GFFT_E_INVALID_PLAN. */
+int gfft_selftest_bounds_check(int* status, int* line);
 
 /* Library version string. */
 const char* gfft_version(void);

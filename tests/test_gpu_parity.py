@@ -523,10 +523,11 @@ def test_multipass_pipelined_matches_engine(cuda, oracle, n, dbl, B):
     dt = np.float64 if dbl else np.float32
     x = inputs.gaussian(91 + n, 2 * n * B).astype(dt)
     for tr in (0, 1):
-        fast = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+        fast = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 4})
         gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
         assert rel(fast, gen) <= tol(n, dbl), (n, tr, rel(fast, gen))
     if n <= 1 << 20:
         ex = oracle.fft_ld(x[:2 * n].astype(np.float64), n, 1, 1)
-        y = run_gpu(cuda, n, vt, 0, 1, x[:2 * n])
-        assert rel(y, ex) <= tol(n, dbl)
+        for opts in (None, {"kernel_variant": 4}):  # the default plan and the prefetching column tiles
+            y = run_gpu(cuda, n, vt, 0, 1, x[:2 * n], opts=opts)
+            assert rel(y, ex) <= tol(n, dbl)

@@ -87,3 +87,24 @@ def test_shipped_cost_model_prunes(cuda):
     assert model is not None
     opts, ms = tuner.choose(model, 3 * 2 ** 18, 1, 0, 1, 8, k=5)
     assert ms > 0 and isinstance(opts, dict)
+
+
+def test_learned_plan_choice_in_the_facade(cuda, oracle):
+    """TransformObject(plan="learned") takes the shipped cost model's first
+    choice, plan="measured" the best measured of its top 5; both transform
+    correctly (exact oracle, FP32 bound)."""
+    import numpy as np
+    from gfft_gb300 import gfft as G
+    from gfft_gb300 import inputs
+    for plan in ("learned", "measured"):
+        for n, b in ((3 * 2 ** 14, 4), (1 << 20, 1), (5 ** 6, 3)):
+            obj = G.TransformObject(n, G.FLOAT, G.DFT, 1, G.Serial, G.OUT_OF_PLACE, b, plan=plan)
+            x = inputs.gaussian(n + b, 2 * n * b).astype(np.float32)
+            xt = cuda.from_numpy(x).cuda()
+            y = cuda.empty_like(xt)
+            obj.fft(xt, y)
+            cuda.cuda.synchronize()
+            ex = oracle.fft_ld(x.astype(np.float64), n, b, 1)
+            got = y.cpu().numpy().astype(np.float64)
+            assert np.linalg.norm(got - ex) / np.linalg.norm(ex) <= 6e-7 * np.log2(n), (plan, n)
+            obj.close()
