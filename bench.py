@@ -763,6 +763,18 @@ def main():
             if rep >= 2:
                 floor.append((time.perf_counter() - t0) * 1e3)
         floor_ms = min(floor)
+        # the host link one direction at a time (pinned buffers, best of three)
+        link = {}
+        for name, dst_, src_ in (("h2d", dx, hx), ("d2h", hy, y)):
+            best = float("inf")
+            for rep in range(4):
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                dst_.copy_(src_, non_blocking=True)
+                torch.cuda.synchronize(dev)
+                if rep >= 1:
+                    best = min(best, time.perf_counter() - t0)
+            link[name + "_gbs"] = nel * 4 / best / 1e9
         del dx
         obj.fft(hx, hy)  # allocates the staging buffer once
         e2e_steps = max(3, min(args.steps, 10))
@@ -774,7 +786,8 @@ def main():
         e2e = {"value": flops(n, batch) * world / (e_ms * 1e-3) / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": nel * 4, "d2h_bytes_per_step": nel * 4, "ms_per_step": e_ms,
                "path": "gfft_exec_host (C ABI): pinned H2D + transform + D2H + stream sync, pipelined in batch slices",
-               "copy_floor_ms": floor_ms}
+               "copy_floor_ms": floor_ms, "host_link": dict(link, both_gbs=2 * nel * 4 / (floor_ms * 1e-3) / 1e9,
+                                                             note="pinned copies measured in this run")}
         del hx, hy
 
     cpu = None

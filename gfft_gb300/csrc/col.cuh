@@ -274,7 +274,7 @@ __device__ __forceinline__ void rd(typename Vec<T>::t (&v)[16], const typename V
 }
 
 template <typename T, int L, int P, bool LF>
-__device__ __forceinline__ void cp(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* __restrict__ tw, int twoff) {
+__device__ __forceinline__ void cp(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* tw, int twoff) {
   typedef Shape<T, L> S;
   typedef typename Vec<T>::t V;
   constexpr int R = radix_of(L, P), Q = 16 / R, NS = ns_of(L, P);
@@ -282,9 +282,9 @@ __device__ __forceinline__ void cp(typename Vec<T>::t (&v)[16], const typename V
   for (int q = 0; q < Q; ++q) {
     if constexpr (NS > 1) {
       const int j = j_of<S::W, S::NT, LF>(q);
-      const V* t = tw + twoff + (j % NS);
+      const V* t = tw + twoff + (j % NS);  // shared memory
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], __ldg(t + (r - 1) * NS));
+      for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], t[(r - 1) * NS]);
     }
     dft<T, V, R>(&v[q * R]);
   }
@@ -313,16 +313,16 @@ __device__ __forceinline__ void wr(const typename Vec<T>::t (&v)[16], typename V
 // the caller synchronises after the last write
 template <typename T, int L, int P>
 __device__ __forceinline__ void middle(typename Vec<T>::t (&v)[16], typename Vec<T>::t* work,
-                                       const typename Vec<T>::t* tw, const BlockPass* bp, int* st) {
+                                       const typename Vec<T>::t* tw, int tw0, const BlockPass* bp, int* st) {
   typedef Shape<T, L> S;
   constexpr int NP = npass_of(L);
   if constexpr (P < NP - 1) {
     if constexpr (P > 1) group_sync<S::W, S::NT>();
     rd<T, L, P, false>(v, work, st);
-    cp<T, L, P, false>(v, tw, bp[P].tw);
+    cp<T, L, P, false>(v, tw, bp[P].tw - tw0);
     group_sync<S::W, S::NT>();
     wr<T, L, P, false>(v, work, st);
-    middle<T, L, P + 1>(v, work, tw, bp, st);
+    middle<T, L, P + 1>(v, work, tw, tw0, bp, st);
   }
 }
 
@@ -359,8 +359,15 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
   extern __shared__ __align__(1024) unsigned char smem[];
   const int S = a.stages;
   V* const work = reinterpret_cast<V*>(smem + (size_t)S * TB);
-  uint64_t* const bars = reinterpret_cast<uint64_t*>(smem + (size_t)S * TB + Gm::WORK);
-  const V* tw = (const V*)a.tw;
+  // the pass's in-block twiddles (L - 1 entries from pass[0].tw on),
+  // copied once per block: shared-memory loads instead of scattered L1 ones
+  constexpr int TWN = colshape::tw_entries(L);
+  V* const stw = reinterpret_cast<V*>(smem + (size_t)S * TB + Gm::WORK);
+  uint64_t* const bars =
+      reinterpret_cast<uint64_t*>(smem + (size_t)S * TB + Gm::WORK + colshape::tw_bytes(esz<T>(), L));
+  const int tw0 = a.pass[0].tw;
+  for (int e = threadIdx.x; e < TWN; e += NT) stw[e] = __ldg((const V*)a.tw + tw0 + e);
+  const V* tw = stw;
   const V* rtw = (const V*)a.rtw;
   const T sc = (T)a.scale;
   const bool conj = a.conj != 0;
@@ -486,12 +493,12 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
     }
     wr<T, L, 0, true>(v, work, a.status);
     __syncthreads();
-    middle<T, L, 1>(v, work, tw, a.pass, a.status);
+    middle<T, L, 1>(v, work, tw, tw0, a.pass, a.status);
     if (gNs == 1) {
       // first global pass: lane groups, each lane's L outputs contiguous
       if constexpr (NP > 2) group_sync<W, NT>();
       rd<T, L, NP - 1, false>(v, work, a.status);
-      cp<T, L, NP - 1, false>(v, tw, a.pass[NP - 1].tw);
+      cp<T, L, NP - 1, false>(v, tw, a.pass[NP - 1].tw - tw0);
       V* o = (V*)a.out + t * a.N;
 #pragma unroll
       for (int q = 0; q < QL; ++q) {
@@ -509,7 +516,7 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
       // later global passes: lane-fastest, dense tile in the work buffer, tensor stores
       if constexpr (NP > 2) __syncthreads();
       rd<T, L, NP - 1, true>(v, work, a.status);
-      cp<T, L, NP - 1, true>(v, tw, a.pass[NP - 1].tw);
+      cp<T, L, NP - 1, true>(v, tw, a.pass[NP - 1].tw - tw0);
       __syncthreads();
 #pragma unroll
       for (int q = 0; q < QL; ++q) {

@@ -52,9 +52,15 @@ constexpr bool supported(int esz, int L, int rf) {
   return L >= 64 && (L & (L - 1)) == 0 && L <= (esz == 16 ? 2048 : 4096) &&
          (!rf || (L <= 2048 && (esz == 16 ? lanes(esz, L) >= 2 : lanes(esz, L) >= 4)));
 }
-// shared memory of a launch with `stages` stages (plus one mbarrier each)
+// in-block twiddles of a pass, sum over its in-block passes of (R - 1) Ns
+// = L - 1 (the product telescopes): the contiguous block of the plan's table
+// that the kernel copies to shared memory
+constexpr int tw_entries(int L) { return L - 1; }
+constexpr int tw_bytes(int esz, int L) { return ((tw_entries(L) * esz + 15) / 16) * 16; }
+// shared memory of a launch with `stages` stages: the stages, the work
+// buffer, the in-block twiddles and one mbarrier per stage
 constexpr long long smem_bytes(int esz, int L, int rf, int stages) {
-  return (long long)stages * stage_bytes(esz, L, rf) + work_bytes_rf(esz, L, rf) + 8LL * stages;
+  return (long long)stages * stage_bytes(esz, L, rf) + work_bytes_rf(esz, L, rf) + tw_bytes(esz, L) + 8LL * stages;
 }
 
 }  // namespace colshape
