@@ -449,10 +449,10 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     if (col_ok && plan.nglobal > 1 && gp.L >= 64 && gp.L <= col_max && spec_radices(gp)) {
       int W = 0, T = 0;
       size_t sm = 0;
-      // two stages for passes up to 256, one above (measured on GB300: the
-      // larger L1 left by one stage serves the twiddle tables of the longer
-      // in-block pass sequences)
-      int S = o.stages > 0 ? o.stages : (gp.L >= 512 ? 1 : 2);
+      // two stages where they fit the shared memory, else one (measured on
+      // GB300 with the in-block twiddles in shared memory: two stages 2-12 %
+      // faster for passes of 128 .. 2048, within 2 % for 1024 x 1024)
+      int S = o.stages > 0 ? o.stages : 2;
       if (gfft_col_shape(dbl, gp.L, S, 0, &W, &T, &sm) == 0 && (n / gp.L) % W == 0 && (g == 0 || Ns % W == 0)) {
         while (S > 1 && sm > 227 * 1024) gfft_col_shape(dbl, gp.L, --S, 0, &W, &T, &sm);
         if (sm <= 227 * 1024) {
@@ -520,9 +520,12 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       const int rf = trans == 2 ? 1 : 2;
       int W = 0, T = 0;
       size_t sm = 0;
-      if (gfft_col_shape(dbl, gp.L, gp.stages, rf, &W, &T, &sm) == 0 && sm <= 227 * 1024 && W >= 2 &&
-          (n / gp.L) % W == 0) {
+      int S = gp.stages;
+      int ok = gfft_col_shape(dbl, gp.L, S, rf, &W, &T, &sm) == 0;
+      while (ok && S > 1 && sm > 227 * 1024) ok = gfft_col_shape(dbl, gp.L, --S, rf, &W, &T, &sm) == 0;
+      if (ok && sm <= 227 * 1024 && W >= 2 && (n / gp.L) % W == 0) {
         gp.rf = rf;
+        gp.stages = S;
         gp.smem = sm;
         plan.real_fused = 1;
       }
