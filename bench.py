@@ -780,12 +780,16 @@ def main():
         e2e_steps = max(3, min(args.steps, 10))
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
+        marks = [t0]
         for _ in range(e2e_steps):
-            obj.fft(hx, hy)
+            obj.fft(hx, hy)  # returns after its own stream synchronisation
+            marks.append(time.perf_counter())
         e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+        e_steps_ms = [round((b - a) * 1e3, 3) for a, b in zip(marks, marks[1:])]
         e2e = {"value": flops(n, batch) * world / (e_ms * 1e-3) / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": nel * 4, "d2h_bytes_per_step": nel * 4, "ms_per_step": e_ms,
                "path": "gfft_exec_host (C ABI): pinned H2D + transform + D2H + stream sync, pipelined in batch slices",
+               "steps_ms": e_steps_ms,
                "copy_floor_ms": floor_ms, "host_link": dict(link, both_gbs=2 * nel * 4 / (floor_ms * 1e-3) / 1e9,
                                                              note="pinned copies measured in this run")}
         del hx, hy

@@ -30,6 +30,7 @@ int parse_opts(const gfft_plan_opts* opts, PlanOpts& po) {
   if (opts->stages < 0 || opts->stages > 8 || opts->blocks_per_sm < 0 || opts->blocks_per_sm > 32)
     return GFFT_E_INVALID_PLAN;
   po.stages = opts->stages;
+  po.bps = opts->blocks_per_sm;
   if (opts->decimation < 0 || opts->decimation > 1) return GFFT_E_INVALID_PLAN;
   if (opts->decimation && opts->kernel_variant && opts->kernel_variant != 1) return GFFT_E_INVALID_PLAN;
   po.dif = opts->decimation;

@@ -77,23 +77,23 @@ using spec::radix_of;
 template <typename T> constexpr int esz() { return (int)sizeof(typename Vec<T>::t); }
 
 // launch shape of a pass (colshape.h: the same arithmetic on the host)
-template <typename T, int L> struct Shape {
+template <typename T, int L, int TK = 64> struct Shape {
   typedef typename Vec<T>::t V;
-  static constexpr int W = colshape::lanes(esz<T>(), L);
+  static constexpr int W = colshape::lanes(esz<T>(), L, TK);
   static constexpr int NT = W * L / 16;
   static constexpr int NP = npass_of(L);
   static constexpr int LP = colshape::lane_stride(esz<T>(), L, W);
   static constexpr int TB = W * L * esz<T>();       // bytes of one tile
   static constexpr int BR = L < 256 ? L : 256;      // rows per tensor box
   static constexpr int NBOX = L / BR;
-  static constexpr int WORK = colshape::work_bytes(esz<T>(), L);
+  static constexpr int WORK = colshape::work_bytes(esz<T>(), L, TK);
 };
 
 // Tile geometry of a pass: RF = 0 one box of W columns; RF = 1, 2 (real
 // pairs) regions A (H = W/2 columns), B (HB columns: the H mirrors, FP32 two
 // wider) and C (HC columns: column S/2), each a dense [L][width] block.
-template <typename T, int L, int RF> struct Geo {
-  static constexpr int W = Shape<T, L>::W;
+template <typename T, int L, int RF, int TK = 64> struct Geo {
+  static constexpr int W = Shape<T, L, TK>::W;
   static constexpr int H = W / 2;
   static constexpr bool F64 = esz<T>() == 16;
   static constexpr int WA = colshape::width_a(esz<T>(), L, RF);
@@ -101,8 +101,8 @@ template <typename T, int L, int RF> struct Geo {
   static constexpr int BOFF = F64 ? 0 : 1;  // first needed column inside region B
   static constexpr int HC = colshape::width_c(esz<T>(), RF);
   static constexpr int OFF_B = WA * L, OFF_C = (WA + HB) * L;  // elements
-  static constexpr int TB = colshape::stage_bytes(esz<T>(), L, RF);
-  static constexpr int WORK = colshape::work_bytes_rf(esz<T>(), L, RF);
+  static constexpr int TB = colshape::stage_bytes(esz<T>(), L, RF, TK);
+  static constexpr int WORK = colshape::work_bytes_rf(esz<T>(), L, RF, TK);
 };
 
 // where lane `lane` of tile p finds its column: smem element offset of row s
@@ -112,9 +112,9 @@ struct LaneSrc {
   int base, width, col;
   long long unit;
 };
-template <typename T, int L, int RF>
+template <typename T, int L, int RF, int TK = 64>
 __device__ __forceinline__ LaneSrc lane_src(int lane, long long p, long long S) {
-  typedef Geo<T, L, RF> G;
+  typedef Geo<T, L, RF, TK> G;
   LaneSrc r;
   if (!RF) {
     r.base = 0;
@@ -256,9 +256,9 @@ template <int W, int NT> __device__ __forceinline__ void group_sync() {
   }
 }
 
-template <typename T, int L, int P, bool LF>
+template <typename T, int L, int P, bool LF, int TK>
 __device__ __forceinline__ void rd(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* buf, int* st) {
-  typedef Shape<T, L> S;
+  typedef Shape<T, L, TK> S;
   constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R;
   (void)st;
 #pragma unroll
@@ -273,9 +273,9 @@ __device__ __forceinline__ void rd(typename Vec<T>::t (&v)[16], const typename V
   }
 }
 
-template <typename T, int L, int P, bool LF>
+template <typename T, int L, int P, bool LF, int TK>
 __device__ __forceinline__ void cp(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* tw, int twoff) {
-  typedef Shape<T, L> S;
+  typedef Shape<T, L, TK> S;
   typedef typename Vec<T>::t V;
   constexpr int R = radix_of(L, P), Q = 16 / R, NS = ns_of(L, P);
 #pragma unroll
@@ -290,9 +290,9 @@ __device__ __forceinline__ void cp(typename Vec<T>::t (&v)[16], const typename V
   }
 }
 
-template <typename T, int L, int P, bool LF>
+template <typename T, int L, int P, bool LF, int TK>
 __device__ __forceinline__ void wr(const typename Vec<T>::t (&v)[16], typename Vec<T>::t* buf, int* st) {
-  typedef Shape<T, L> S;
+  typedef Shape<T, L, TK> S;
   constexpr int R = radix_of(L, P), Q = 16 / R, NS = ns_of(L, P);
   (void)st;
 #pragma unroll
@@ -311,18 +311,18 @@ __device__ __forceinline__ void wr(const typename Vec<T>::t (&v)[16], typename V
 
 // in-block passes P .. NP-2 with lane groups, in place on the work buffer;
 // the caller synchronises after the last write
-template <typename T, int L, int P>
+template <typename T, int L, int P, int TK>
 __device__ __forceinline__ void middle(typename Vec<T>::t (&v)[16], typename Vec<T>::t* work,
                                        const typename Vec<T>::t* tw, int tw0, const BlockPass* bp, int* st) {
-  typedef Shape<T, L> S;
+  typedef Shape<T, L, TK> S;
   constexpr int NP = npass_of(L);
   if constexpr (P < NP - 1) {
     if constexpr (P > 1) group_sync<S::W, S::NT>();
-    rd<T, L, P, false>(v, work, st);
-    cp<T, L, P, false>(v, tw, bp[P].tw - tw0);
+    rd<T, L, P, false, TK>(v, work, st);
+    cp<T, L, P, false, TK>(v, tw, bp[P].tw - tw0);
     group_sync<S::W, S::NT>();
-    wr<T, L, P, false>(v, work, st);
-    middle<T, L, P + 1>(v, work, tw, tw0, bp, st);
+    wr<T, L, P, false, TK>(v, work, st);
+    middle<T, L, P + 1, TK>(v, work, tw, tw0, bp, st);
   }
 }
 
@@ -342,12 +342,12 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
 }  // namespace col
 
 
-template <typename T, int L, int RF>
-__global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
+template <typename T, int L, int RF, int TK = 64>
+__global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
     col_kernel(const __grid_constant__ EngineArgs a, const __grid_constant__ col::ColMaps maps) {
   using namespace col;
-  typedef Shape<T, L> Sh;
-  typedef Geo<T, L, RF> Gm;
+  typedef Shape<T, L, TK> Sh;
+  typedef Geo<T, L, RF, TK> Gm;
   typedef typename Vec<T>::t V;
   constexpr int W = Sh::W, NT = Sh::NT, NP = Sh::NP, TB = Gm::TB, BR = Sh::BR, NBOX = Sh::NBOX;
   constexpr int NB0 = L / radix_of(L, 0);  // first pass: radix 16, one butterfly per thread
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
     // first in-block pass, lane-fastest: lane = tid % W, j = tid / W
     {
       const int lane = threadIdx.x % W, j = threadIdx.x / W;
-      const LaneSrc src = lane_src<T, L, RF>(lane, p, stride);
+      const LaneSrc src = lane_src<T, L, RF, TK>(lane, p, stride);
       const V* sp = st + src.base + src.col;
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
@@ -491,19 +491,19 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
       const long long nt = tile + (long long)S * G;
       if (nt < a.ntiles) issue(nt, s);
     }
-    wr<T, L, 0, true>(v, work, a.status);
+    wr<T, L, 0, true, TK>(v, work, a.status);
     __syncthreads();
-    middle<T, L, 1>(v, work, tw, tw0, a.pass, a.status);
+    middle<T, L, 1, TK>(v, work, tw, tw0, a.pass, a.status);
     if (gNs == 1) {
       // first global pass: lane groups, each lane's L outputs contiguous
       if constexpr (NP > 2) group_sync<W, NT>();
-      rd<T, L, NP - 1, false>(v, work, a.status);
-      cp<T, L, NP - 1, false>(v, tw, a.pass[NP - 1].tw - tw0);
+      rd<T, L, NP - 1, false, TK>(v, work, a.status);
+      cp<T, L, NP - 1, false, TK>(v, tw, a.pass[NP - 1].tw - tw0);
       V* o = (V*)a.out + t * a.N;
 #pragma unroll
       for (int q = 0; q < QL; ++q) {
         const int lane = lane_of<W, NT, false>(q), j = j_of<W, NT, false>(q);
-        const long long e0 = t * a.N + lane_src<T, L, RF>(lane, p, stride).unit * L + j;
+        const long long e0 = t * a.N + lane_src<T, L, RF, TK>(lane, p, stride).unit * L + j;
         V* d = (V*)a.out + e0;
 #pragma unroll
         for (int r = 0; r < RL; ++r) {
@@ -515,13 +515,13 @@ __global__ void __launch_bounds__(col::Shape<T, L>::NT, 1)
     } else {
       // later global passes: lane-fastest, dense tile in the work buffer, tensor stores
       if constexpr (NP > 2) __syncthreads();
-      rd<T, L, NP - 1, true>(v, work, a.status);
-      cp<T, L, NP - 1, true>(v, tw, a.pass[NP - 1].tw - tw0);
+      rd<T, L, NP - 1, true, TK>(v, work, a.status);
+      cp<T, L, NP - 1, true, TK>(v, tw, a.pass[NP - 1].tw - tw0);
       __syncthreads();
 #pragma unroll
       for (int q = 0; q < QL; ++q) {
         const int lane = lane_of<W, NT, true>(q), j = j_of<W, NT, true>(q);
-        const LaneSrc dsrc = lane_src<T, L, RF>(lane, p, stride);
+        const LaneSrc dsrc = lane_src<T, L, RF, TK>(lane, p, stride);
 #pragma unroll
         for (int r = 0; r < RL; ++r) {
           V x = v[q * RL + r];

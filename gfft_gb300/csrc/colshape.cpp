@@ -5,14 +5,15 @@
 #include "colshape.h"
 
 // Shape of the variant-9 pass of length L (rf: 0 complex, 1 / 2 real
-// forward post / inverse pre pass): units per tile, threads, and the shared
-// memory of `stages` stages; 1 if L (or the real pass) has no kernel.
-extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int* units, int* threads, size_t* smem) {
+// forward post / inverse pre pass; tk: tile KB, 64 or 32): units per tile,
+// threads, and the shared memory of `stages` stages; 1 if L (or the real
+// pass, or the tile size) has no kernel.
+extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int tk, int* units, int* threads, size_t* smem) {
   using namespace gfft::colshape;
   const int esz = dbl ? 16 : 8;
-  if (!supported(esz, L, rf) || stages < 1 || !units || !threads || !smem) return 1;
-  *units = lanes(esz, L);
-  *threads = gfft::colshape::threads(esz, L);
-  *smem = (size_t)smem_bytes(esz, L, rf, stages);
+  if (!supported(esz, L, rf, tk) || stages < 1 || !units || !threads || !smem) return 1;
+  *units = lanes(esz, L, tk);
+  *threads = gfft::colshape::threads(esz, L, tk);
+  *smem = (size_t)smem_bytes(esz, L, rf, stages, tk);
   return 0;
 }

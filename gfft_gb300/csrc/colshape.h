@@ -1,8 +1,9 @@
 // Shape arithmetic of the tensor-copy column tiles (variant 9), shared by the
 // kernels (col.cuh) and the host (planner.cpp, colshape.cpp).  Plain
 // constexpr functions of the element size (8: FP32 complex, 16: FP64
-// complex), the pass length L and, for the real-pair tiles, rf (0 complex,
-// 1 forward post pass, 2 inverse pre pass): no CUDA types.
+// complex), the pass length L, the tile size tk in KB (64: one block per SM,
+// 32: two) and, for the real-pair tiles, rf (0 complex, 1 forward post pass,
+// 2 inverse pre pass): no CUDA types.
 #pragma once
 
 namespace gfft {
@@ -10,9 +11,9 @@ namespace colshape {
 
 // in-lane padding of the work buffer: one slot per 2^ps elements
 constexpr int ps(int esz) { return esz == 16 ? 3 : 4; }
-// units per tile: tiles of about 64 KB, rows of at least 2 units, at most 64
-constexpr int lanes(int esz, int L) {
-  return (65536 / esz) / L > 64 ? 64 : ((65536 / esz) / L < 2 ? 2 : (65536 / esz) / L);
+// units per tile: tiles of about tk KB, rows of at least 2 units, at most 64
+constexpr int lanes(int esz, int L, int tk = 64) {
+  return (tk * 1024 / esz) / L > 64 ? 64 : ((tk * 1024 / esz) / L < 2 ? 2 : (tk * 1024 / esz) / L);
 }
 // Lane stride of the padded work buffer (elements).  Shared memory serves an
 // 8-byte request per half-warp (16 threads, 16 slots of 8 bytes) and a
@@ -29,28 +30,34 @@ constexpr int lane_stride(int esz, int L, int W) {
 }
 constexpr int round1k(int b) { return ((b + 1023) / 1024) * 1024; }
 // threads: one radix-16 butterfly (16 values) each
-constexpr int threads(int esz, int L) { return lanes(esz, L) * L / 16; }
+constexpr int threads(int esz, int L, int tk = 64) { return lanes(esz, L, tk) * L / 16; }
 // bytes of the padded work buffer of a complex pass
-constexpr int work_bytes(int esz, int L) { return round1k(lanes(esz, L) * lane_stride(esz, L, lanes(esz, L)) * esz); }
+constexpr int work_bytes(int esz, int L, int tk = 64) {
+  return round1k(lanes(esz, L, tk) * lane_stride(esz, L, lanes(esz, L, tk)) * esz);
+}
 // real-pair tiles: region widths (A: W/2 columns, B: the mirrors, FP32 two
 // wider so that its box starts on an even column, C: column S/2)
 constexpr int half(int esz, int L) { return lanes(esz, L) / 2; }
 constexpr int width_b(int esz, int L, int rf) { return rf ? (esz == 16 ? half(esz, L) : half(esz, L) + 2) : 0; }
 constexpr int width_c(int esz, int rf) { return rf ? (esz == 16 ? 1 : 2) : 0; }
 constexpr int width_a(int esz, int L, int rf) { return rf ? half(esz, L) : lanes(esz, L); }
-// bytes of one stage, and of the work buffer (it also holds a dense tile)
-constexpr int stage_bytes(int esz, int L, int rf) {
-  return (width_a(esz, L, rf) + width_b(esz, L, rf) + width_c(esz, rf)) * L * esz;
+// bytes of one stage, and of the work buffer (it also holds a dense tile);
+// real-pair tiles exist with 64 KB tiles only
+constexpr int stage_bytes(int esz, int L, int rf, int tk = 64) {
+  return rf ? (width_a(esz, L, rf) + width_b(esz, L, rf) + width_c(esz, rf)) * L * esz : lanes(esz, L, tk) * L * esz;
 }
-constexpr int work_bytes_rf(int esz, int L, int rf) {
-  return work_bytes(esz, L) > round1k(stage_bytes(esz, L, rf)) ? work_bytes(esz, L) : round1k(stage_bytes(esz, L, rf));
+constexpr int work_bytes_rf(int esz, int L, int rf, int tk = 64) {
+  return work_bytes(esz, L, tk) > round1k(stage_bytes(esz, L, rf, tk)) ? work_bytes(esz, L, tk)
+                                                                     : round1k(stage_bytes(esz, L, rf, tk));
 }
 // pass lengths with a kernel: powers of two 64 .. 4096 (FP32) / 2048 (FP64);
 // real-pair tiles need two units of each kind (W >= 4 for FP32: an even first
-// column of region A)
-constexpr bool supported(int esz, int L, int rf) {
+// column of region A); 32 KB tiles for FP32 complex passes of 128 .. 512
+// (rows of 64 bytes or more)
+constexpr bool supported(int esz, int L, int rf, int tk = 64) {
   return L >= 64 && (L & (L - 1)) == 0 && L <= (esz == 16 ? 2048 : 4096) &&
-         (!rf || (L <= 2048 && (esz == 16 ? lanes(esz, L) >= 2 : lanes(esz, L) >= 4)));
+         (!rf || (L <= 2048 && (esz == 16 ? lanes(esz, L) >= 2 : lanes(esz, L) >= 4))) &&
+         (tk == 64 || (tk == 32 && esz == 8 && !rf && L >= 128 && L <= 512));
 }
 // in-block twiddles of a pass, sum over its in-block passes of (R - 1) Ns
 // = L - 1 (the product telescopes): the contiguous block of the plan's table
@@ -59,8 +66,9 @@ constexpr int tw_entries(int L) { return L - 1; }
 constexpr int tw_bytes(int esz, int L) { return ((tw_entries(L) * esz + 15) / 16) * 16; }
 // shared memory of a launch with `stages` stages: the stages, the work
 // buffer, the in-block twiddles and one mbarrier per stage
-constexpr long long smem_bytes(int esz, int L, int rf, int stages) {
-  return (long long)stages * stage_bytes(esz, L, rf) + work_bytes_rf(esz, L, rf) + tw_bytes(esz, L) + 8LL * stages;
+constexpr long long smem_bytes(int esz, int L, int rf, int stages, int tk = 64) {
+  return (long long)stages * stage_bytes(esz, L, rf, tk) + work_bytes_rf(esz, L, rf, tk) + tw_bytes(esz, L) +
+         8LL * stages;
 }
 
 }  // namespace colshape

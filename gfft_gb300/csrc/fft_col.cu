@@ -48,7 +48,17 @@ int encode(CUtensorMap* m, const void* base, long long rows, long long cols, int
 }
 
 template <typename T>
-const void* col_fn(int L) {
+const void* col_fn(int L, int tk) {
+  if (tk == 32) {  // half-size tiles: FP32 passes of 128 .. 512
+    if (sizeof(T) != 4) return nullptr;
+    switch (L) {
+      case 128: return (const void*)gfft::col_kernel<float, 128, 0, 32>;
+      case 256: return (const void*)gfft::col_kernel<float, 256, 0, 32>;
+      case 512: return (const void*)gfft::col_kernel<float, 512, 0, 32>;
+      default: return nullptr;
+    }
+  }
+  if (tk != 64) return nullptr;
   switch (L) {
     case 64: return (const void*)gfft::col_kernel<T, 64, 0>;
     case 128: return (const void*)gfft::col_kernel<T, 128, 0>;
@@ -60,25 +70,26 @@ const void* col_fn(int L) {
     default: return nullptr;
   }
 }
-const void* kernel_of(int dbl, int L, int rf) {
-  if (rf) return gfft_col_real_fn(dbl, L, rf);
-  return dbl ? col_fn<double>(L) : col_fn<float>(L);
+const void* kernel_of(int dbl, int L, int rf, int tk) {
+  if (rf) return tk == 64 ? gfft_col_real_fn(dbl, L, rf) : nullptr;
+  return dbl ? col_fn<double>(L, tk) : col_fn<float>(L, tk);
 }
 }  // namespace
 
 extern "C" int gfft_col_setup(int dbl, size_t max_smem) {
   if (get_encoder() != 0) return 1;
   int e = 0;
-  for (int rf = 0; rf < 3; ++rf)
-    for (int L : {64, 128, 256, 512, 1024, 2048, 4096}) {
-      const void* f = kernel_of(dbl, L, rf);
-      if (f) e |= cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem) != cudaSuccess;
-    }
+  for (int tk : {64, 32})
+    for (int rf = 0; rf < 3; ++rf)
+      for (int L : {64, 128, 256, 512, 1024, 2048, 4096}) {
+        const void* f = kernel_of(dbl, L, rf, tk);
+        if (f) e |= cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem) != cudaSuccess;
+      }
   return e;
 }
 
-extern "C" int gfft_col_occupancy(int dbl, int L, int rf, int threads, size_t smem) {
-  const void* f = kernel_of(dbl, L, rf);
+extern "C" int gfft_col_occupancy(int dbl, int L, int rf, int tk, int threads, size_t smem) {
+  const void* f = kernel_of(dbl, L, rf, tk);
   if (!f) return 0;
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem);
@@ -88,14 +99,15 @@ extern "C" int gfft_col_occupancy(int dbl, int L, int rf, int threads, size_t sm
 // One global pass: tensor maps of this launch's input and output, then the
 // launch.  Requirements (checked by the planner): N a power of two, the
 // units per tile dividing N / L and Ns, 16-byte aligned buffers; a real pass
-// (a->real) is the last (forward) or first (inverse) pass.
-extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+// (a->real) is the last (forward) or first (inverse) pass; tk the tile KB.
+extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, int tk, unsigned grid, unsigned threads, size_t smem,
                                cudaStream_t stream) {
   const int rf = a->real;
-  const void* f = kernel_of(dbl, a->L, rf);
+  const void* f = kernel_of(dbl, a->L, rf, tk);
   if (!f || !g_encode) return (int)cudaErrorInvalidValue;
   const int esz = dbl ? 16 : 8;
-  const int W = gfft::colshape::lanes(esz, a->L);
+  const int W = gfft::colshape::lanes(esz, a->L, tk);
+  if ((int)threads != gfft::colshape::threads(esz, a->L, tk)) return (int)cudaErrorInvalidValue;
   const long long batch = a->nunits / a->stride;
   const int br = a->L < 256 ? a->L : 256;
   if ((((uintptr_t)a->in) | ((uintptr_t)a->out)) & 15) return (int)cudaErrorInvalidValue;

@@ -7,7 +7,8 @@
 // template parameter: the pass radices, butterfly strides and twiddle strides
 // are compile-time constants, so every shared-memory access is a register
 // base plus an immediate offset and the index arithmetic per leg vanishes.
-// The tile holds 4096 (FP32) or 2048 (FP64) complex values, W = tile / L.
+// The tile holds 4096 (FP32) or 2048 (FP64) complex values, W = tile / L;
+// FP32 8192 runs one transform per tile with 512 threads.
 //
 // Pass order for L = 2^a: radix 16 while four bits remain, then 8 / 4 / 2,
 // matching the planner's default (planner.cpp block_radices).
@@ -22,11 +23,11 @@
 namespace gfft {
 
 template <typename T, int L>
-__global__ void __launch_bounds__(spec::Cfg<T>::TILE / 16, 1) spec_kernel(const __grid_constant__ EngineArgs a) {
+__global__ void __launch_bounds__(spec::tile_of<T>(L) / 16, 1) spec_kernel(const __grid_constant__ EngineArgs a) {
   using namespace spec;
   using namespace fast;
   typedef typename Vec<T>::t V;
-  constexpr int TILE = Cfg<T>::TILE, W = TILE / L, NP = npass_of(L);
+  constexpr int TILE = tile_of<T>(L), W = TILE / L, NP = npass_of(L);
   constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
   constexpr int TB = TILE * (int)sizeof(V);  // bytes of a full tile (multiple of 128)
   extern __shared__ __align__(128) unsigned char smem[];
@@ -231,12 +232,13 @@ const void* spec_fn(int L) {
     case 1024: return (const void*)gfft::spec_kernel<T, 1024>;
     case 2048: return (const void*)gfft::spec_kernel<T, 2048>;
     case 4096: return sizeof(T) == 4 ? (const void*)gfft::spec_kernel<float, 4096> : nullptr;
+    case 8192: return sizeof(T) == 4 ? (const void*)gfft::spec_kernel<float, 8192> : nullptr;
     default: return nullptr;
   }
 }
 }  // namespace
 
-// lengths with a specialised kernel: FP32 16..4096, FP64 16..2048
+// lengths with a specialised kernel: FP32 16..8192, FP64 16..2048
 extern "C" int gfft_spec_supported(int dbl, int L) {
   return (dbl ? spec_fn<double>(L) : spec_fn<float>(L)) != nullptr;
 }
@@ -245,6 +247,7 @@ extern "C" int gfft_spec_setup(int dbl, size_t max_smem) {
   if (dbl) return spec_setup_all<double>(max_smem);
   int e = spec_setup_all<float>(max_smem);
   e |= spec_setup_one<float, 4096>(max_smem);
+  e |= spec_setup_one<float, 8192>(max_smem);
   return e;
 }
 

@@ -48,8 +48,8 @@ extern "C" int gfft_tc_setup(size_t max_smem);
 extern "C" int gfft_tc_occupancy(int L, int threads, size_t smem);
 extern "C" int gfft_tc_launch(const EngineArgs* a, unsigned grid, unsigned threads, size_t smem, cudaStream_t stream);
 extern "C" int gfft_col_setup(int dbl, size_t max_smem);
-extern "C" int gfft_col_occupancy(int dbl, int L, int rf, int threads, size_t smem);
-extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+extern "C" int gfft_col_occupancy(int dbl, int L, int rf, int tk, int threads, size_t smem);
+extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, int tk, unsigned grid, unsigned threads, size_t smem,
                                cudaStream_t stream);
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
@@ -180,7 +180,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)
                        : gp.variant == 7 ? mixed_occupancy(dbl, gp)
-                       : gp.variant == 9 ? gfft_col_occupancy(dbl, gp.L, gp.rf, gp.threads, gp.smem)
+                       : gp.variant == 9 ? gfft_col_occupancy(dbl, gp.L, gp.rf, gp.tk, gp.threads, gp.smem)
                                          : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
       if (gp.variant == 6 && !(opts && opts->blocks_per_sm)) {
         // two blocks fit by registers (launch bound) and shared memory whenever
@@ -404,7 +404,8 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
       a.ntiles = gp.ntiles;
       a.stages = gp.stages;
       a.spin_limit = 1LL << 26;
-      if (gfft_col_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0) return GFFT_E_CUDA;
+      if (gfft_col_launch(dbl, &a, gp.tk, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0)
+        return GFFT_E_CUDA;
       continue;
     }
     if (gp.variant == 7) {

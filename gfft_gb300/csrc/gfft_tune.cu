@@ -54,7 +54,7 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   const int variants[] = {0, 1};
   const int caps[] = {0, 4096, 1024, 256, 64};
   struct K {
-    int cap, v, mr, ro, st, w;
+    int cap, v, mr, ro, st, w, bps = 0;
   };
   std::vector<K> ks;
   // pipeline depths other than the default (one stage FP32, two FP64)
@@ -62,6 +62,8 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   ks.push_back({0, 0, 16, 0, 0, 0});
   for (int st : {1, 2, 3})
     if (st != dflt_st) ks.push_back({0, 0, 16, 0, st, 0});
+  // 64 KB tensor-copy tiles where FP32 passes of 128 .. 512 default to 32 KB
+  for (int cap : {0, 4096, 1024}) ks.push_back({cap, 0, 16, 0, 0, 0, 1});
   // wider column tiles (128- and 256-byte rows) with shorter passes
   for (int cap : {0, 512, 256, 128})
     for (int w : {16, 32}) ks.push_back({cap, 0, 16, 0, 0, w});
@@ -82,6 +84,7 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
     o.stages = k.st;
     o.max_pass_len = k.cap;
     o.units_per_block = k.w;
+    o.blocks_per_sm = k.bps;
     gfft_plan_info info;
     if (gfft_plan_query(n, vtype_id, trans_id, place_id, batch, &o, &info) != GFFT_OK) continue;
     if (k.w != 0) {  // a lane width only where the column-tile kernel runs

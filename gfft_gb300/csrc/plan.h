@@ -116,6 +116,7 @@ struct GlobalPass {
   size_t smem;
   int stages;     // variant 2: TMA pipeline depth
   int rf = 0;     // variant 9: real pre (2) / post (1) pass fused into this pass
+  int tk = 64;    // variant 9: tile KB (64: one block per SM, 32: two)
   long long ntiles;
   int tile_bytes;
 };
@@ -132,6 +133,7 @@ struct PlanOpts {
   int max_single = 0;
   int smem_budget = 0;
   int dif = 0;  // frequency decimation (generic engine only)
+  int bps = 0;  // requested blocks per SM (1: 64 KB column tiles for every pass)
 };
 
 // ---- ragged batches: one persistent launch over transforms of many sizes --

@@ -27,7 +27,7 @@
 
 bool spec_radices(const GlobalPass& gp);
 // fft_col.cu: launch shape of the tensor-copy column tiles (variant 9)
-extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int* units, int* threads, size_t* smem);
+extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int tk, int* units, int* threads, size_t* smem);
 
 namespace {
 
@@ -449,17 +449,24 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     if (col_ok && plan.nglobal > 1 && gp.L >= 64 && gp.L <= col_max && spec_radices(gp)) {
       int W = 0, T = 0;
       size_t sm = 0;
-      // two stages where they fit the shared memory, else one (measured on
-      // GB300 with the in-block twiddles in shared memory: two stages 2-12 %
-      // faster for passes of 128 .. 2048, within 2 % for 1024 x 1024)
-      int S = o.stages > 0 ? o.stages : 2;
-      if (gfft_col_shape(dbl, gp.L, S, 0, &W, &T, &sm) == 0 && (n / gp.L) % W == 0 && (g == 0 || Ns % W == 0)) {
-        while (S > 1 && sm > 227 * 1024) gfft_col_shape(dbl, gp.L, --S, 0, &W, &T, &sm);
+      // FP32 passes of 128 .. 512: half-size (32 KB) tiles, one stage, two
+      // blocks per SM (measured on GB300 against 64 KB tiles with two
+      // stages: 4-6 % faster for 2^17 .. 2^19 and 2^23 .. 2^24, within 2 %
+      // for 2^14 .. 2^16); blocks_per_sm = 1 keeps the 64 KB tiles.  Other
+      // passes: two stages where they fit the shared memory, else one (two
+      // stages 2-12 % faster for passes of 128 .. 2048 with 64 KB tiles,
+      // within 2 % for 1024 x 1024).
+      int tk = 64;
+      if (o.bps != 1 && gfft_col_shape(dbl, gp.L, 1, 0, 32, &W, &T, &sm) == 0) tk = 32;
+      int S = o.stages > 0 ? o.stages : (tk == 32 ? 1 : 2);
+      if (gfft_col_shape(dbl, gp.L, S, 0, tk, &W, &T, &sm) == 0 && (n / gp.L) % W == 0 && (g == 0 || Ns % W == 0)) {
+        while (S > 1 && sm > 227 * 1024) gfft_col_shape(dbl, gp.L, --S, 0, tk, &W, &T, &sm);
         if (sm <= 227 * 1024) {
           gp.variant = 9;
           gp.units = W;
           gp.threads = T;
           gp.stages = S;
+          gp.tk = tk;
           gp.smem = sm;
           gp.ntiles = batch * (n / gp.L) / W;
         }
@@ -480,17 +487,23 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       gp.ntiles = 0;
     }
     // length-specialised variant: default radix order, L in the compiled set
+    // (FP32 8192: one transform per tile, 512 threads)
     bool spec = gp.variant == 2 && (o.variant == 0 || o.variant == 3) && o.units == 0 && o.threads == 0 &&
-                gp.L <= TILE && o.radix_order == 0 && o.max_radix == 16;
+                (gp.L <= TILE || (!dbl && gp.L == 8192)) && o.radix_order == 0 && o.max_radix == 16;
     if (spec) {
-      const long long W = TILE / gp.L;
+      const long long SPT = std::max<long long>(TILE, gp.L);
+      const long long W = SPT / gp.L;
       gp.variant = 3;
       gp.units = (int)W;
-      gp.threads = (int)(TILE / 16);
-      gp.tile_bytes = (int)(TILE * esz);
+      gp.threads = (int)(SPT / 16);
+      gp.tile_bytes = (int)(SPT * esz);
       gp.ntiles = (batch + W - 1) / W;
-      const int S = gp.stages;
-      gp.smem = (size_t)(S * TILE * esz + ((W * padded(gp.L) * esz + 7) & ~7LL) + 8 * S);
+      // 8192: one stage (measured 5 % faster than two; the copy of the next
+      // tile overlaps the passes after the first)
+      int S = gp.stages;
+      while (S > 1 && S * SPT * esz + W * padded(gp.L) * esz + 8 * S > 220 * 1024) --S;
+      gp.stages = S;
+      gp.smem = (size_t)(S * SPT * esz + ((W * padded(gp.L) * esz + 7) & ~7LL) + 8 * S);
     }
     Ns *= gp.L;
   }
@@ -516,15 +529,20 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
     bool all9 = plan.nglobal > 1;
     for (int g = 0; g < plan.nglobal; ++g) all9 = all9 && plan.gp[g].variant == 9;
     if (all9) {
+      // real-pair tiles exist with 64 KB tiles only: the fused pass takes them
       GlobalPass& gp = plan.gp[trans == 2 ? plan.nglobal - 1 : 0];
       const int rf = trans == 2 ? 1 : 2;
       int W = 0, T = 0;
       size_t sm = 0;
-      int S = gp.stages;
-      int ok = gfft_col_shape(dbl, gp.L, S, rf, &W, &T, &sm) == 0;
-      while (ok && S > 1 && sm > 227 * 1024) ok = gfft_col_shape(dbl, gp.L, --S, rf, &W, &T, &sm) == 0;
+      int S = gp.tk == 32 && o.stages == 0 ? 2 : gp.stages;
+      int ok = gfft_col_shape(dbl, gp.L, S, rf, 64, &W, &T, &sm) == 0;
+      while (ok && S > 1 && sm > 227 * 1024) ok = gfft_col_shape(dbl, gp.L, --S, rf, 64, &W, &T, &sm) == 0;
       if (ok && sm <= 227 * 1024 && W >= 2 && (n / gp.L) % W == 0) {
         gp.rf = rf;
+        gp.tk = 64;
+        gp.units = W;
+        gp.threads = T;
+        gp.ntiles = batch * (n / gp.L) / W;
         gp.stages = S;
         gp.smem = sm;
         plan.real_fused = 1;

@@ -1,10 +1,11 @@
 // Compile-time Stockham passes shared by the length-specialised kernels
 // (fft_spec.cu) and the tensor-core split-precision kernel (fft_tc.cu).
 //
-// A tile holds 4096 (FP32) or 2048 (FP64) complex values: W = tile / L
-// transforms (or column lanes) of a power-of-two length L, in a padded
-// [lane][pad(s)] shared buffer.  Each of tile / 16 threads keeps 16 values
-// in registers: 16 / R butterflies of radix R per pass.  Pass order for
+// A tile holds 4096 (FP32) or 2048 (FP64) complex values, or one transform
+// of a longer L (tile_of): W = tile / L transforms (or column lanes) of a
+// power-of-two length L, in a padded [lane][pad(s)] shared buffer.  Each of
+// tile / 16 threads keeps 16 values in registers: 16 / R butterflies of
+// radix R per pass.  Pass order for
 // L = 2^a: radix 16 while four bits remain, then 8 / 4 / 2, matching the
 // planner's default (planner.cpp block_radices).
 #pragma once
@@ -39,12 +40,15 @@ template <> struct Cfg<double> {
   static constexpr int PS = 3;
 };
 
+// complex values per tile for length L: the type's tile, or one transform
+template <typename T> constexpr int tile_of(int L) { return L > Cfg<T>::TILE ? L : Cfg<T>::TILE; }
+
 template <typename T> __device__ __forceinline__ constexpr int padi(int s) { return s + (s >> Cfg<T>::PS); }
 
 // pass P: read the legs of this thread's butterflies
 template <typename T, int L, int P, bool FROM_STAGE>
 __device__ __forceinline__ void sread(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* src) {
-  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NT = Cfg<T>::TILE / 16;
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NT = tile_of<T>(L) / 16;
   constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -67,7 +71,7 @@ template <typename T, int L, int P>
 __device__ __forceinline__ void scompute(typename Vec<T>::t (&v)[16], const typename Vec<T>::t* __restrict__ tw,
                                          int twoff) {
   typedef typename Vec<T>::t V;
-  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NS = ns_of(L, P), NT = Cfg<T>::TILE / 16;
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NS = ns_of(L, P), NT = tile_of<T>(L) / 16;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     if constexpr (NS > 1) {
@@ -82,7 +86,7 @@ __device__ __forceinline__ void scompute(typename Vec<T>::t (&v)[16], const type
 
 template <typename T, int L, int P>
 __device__ __forceinline__ void swrite(const typename Vec<T>::t (&v)[16], typename Vec<T>::t* work) {
-  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NS = ns_of(L, P), NT = Cfg<T>::TILE / 16;
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NS = ns_of(L, P), NT = tile_of<T>(L) / 16;
   constexpr int LP = L + (L >> Cfg<T>::PS) + 1;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -101,7 +105,7 @@ template <typename T, int L, int P>
 __device__ __forceinline__ void sstore(const typename Vec<T>::t (&v)[16], typename Vec<T>::t* out, int units,
                                        bool conj, T sc) {
   typedef typename Vec<T>::t V;
-  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NT = Cfg<T>::TILE / 16;
+  constexpr int R = radix_of(L, P), NB = L / R, Q = 16 / R, NT = tile_of<T>(L) / 16;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int b = threadIdx.x + q * NT;

@@ -80,6 +80,19 @@ class MLP:
     def _fp(a):
         return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
+    def _rows(self, X, y=None):
+        """X as C-contiguous FP32 rows of exactly `nin` features (the library
+        reads len(X) * nin values), y one target per row."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        if X.ndim != 2 or X.shape[1] != self.nin:
+            raise ValueError("features must have shape (rows, %d), got %s" % (self.nin, X.shape))
+        if y is None:
+            return X
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        if y.shape != (len(X),):
+            raise ValueError("targets must have shape (%d,), got %s" % (len(X), y.shape))
+        return X, y
+
     def params(self):
         p = np.zeros(self.nparams, dtype=np.float32)
         _lib.check(_lib.lib().gfft_mlp_get_params(self._h, self._fp(p)))
@@ -90,22 +103,20 @@ class MLP:
         _lib.check(_lib.lib().gfft_mlp_set_params(self._h, self._fp(p)))
 
     def train(self, X, y, epochs=2000, lr=3e-3):
-        X = np.ascontiguousarray(X, dtype=np.float32)
-        y = np.ascontiguousarray(y, dtype=np.float32)
+        X, y = self._rows(X, y)
         loss = ctypes.c_float()
         _lib.check(_lib.lib().gfft_mlp_train(self._h, self._fp(X), self._fp(y), len(y), epochs, lr,
                                              ctypes.byref(loss)), "gfft_mlp_train")
         return loss.value
 
     def predict(self, X):
-        X = np.ascontiguousarray(X, dtype=np.float32)
+        X = self._rows(X)
         out = np.zeros(len(X), dtype=np.float32)
         _lib.check(_lib.lib().gfft_mlp_predict(self._h, self._fp(X), len(X), self._fp(out)), "gfft_mlp_predict")
         return out
 
     def gradients(self, X, y):
-        X = np.ascontiguousarray(X, dtype=np.float32)
-        y = np.ascontiguousarray(y, dtype=np.float32)
+        X, y = self._rows(X, y)
         g = np.zeros(self.nparams, dtype=np.float32)
         loss = ctypes.c_float()
         _lib.check(_lib.lib().gfft_mlp_gradients(self._h, self._fp(X), self._fp(y), len(y), self._fp(g),

@@ -69,6 +69,12 @@ def test_plan_shapes(n, vt, passes):
 def test_plan_power_of_two_uses_radix16():
     d = _lib.plan_query(4096, 1, 0, 1, 65536)
     assert d["radices"] == [[16, 16, 16]]
+    # FP32 8192: the length-specialised single pass, one transform per tile,
+    # 512 threads, two stages; variant 2 on request
+    d = _lib.plan_query(8192, 1, 0, 1, 100)
+    assert d["kernel_variant"] == [3] and d["threads"] == [512] and d["units"] == [1], d
+    assert d["radices"] == [[16, 16, 8, 4]]
+    assert _lib.plan_query(8192, 1, 0, 1, 100, {"kernel_variant": 2})["kernel_variant"] == [2]
     d = _lib.plan_query(4096, 1, 0, 1, 1, {"max_radix": 4})
     assert d["radices"] == [[4] * 6]
 
@@ -84,10 +90,14 @@ def test_plan_column_kernel_selection():
         d = _lib.plan_query(n, vt, 0, 1, 1)
         assert d["n_global_passes"] == passes and set(d["kernel_variant"]) == {9}, (n, vt, d)
         assert all(64 <= L <= 2048 for L in d["pass_len"][:passes])
-        # tiles of about 64 KB: units = 64 KB / (L * element size), 2 .. 64
+        # tiles of about 64 KB: units = 64 KB / (L * element size), 2 .. 64;
+        # FP32 passes of 128 .. 512: 32 KB tiles (64 KB with blocks_per_sm 1)
         esz = 16 if vt == 0 else 8
-        for L, W in zip(d["pass_len"][:passes], d["units"][:passes]):
-            assert W == max(2, min(64, 65536 // esz // L)), (L, W)
+        d1 = _lib.plan_query(n, vt, 0, 1, 1, {"blocks_per_sm": 1})
+        for L, W, W1 in zip(d["pass_len"][:passes], d["units"][:passes], d1["units"][:passes]):
+            assert W1 == max(2, min(64, 65536 // esz // L)), (L, W1)
+            half = esz == 8 and 128 <= L <= 512
+            assert W == (W1 // 2 if half else W1), (L, W, W1)
     # two passes of 4096 x 4096 on request
     d = _lib.plan_query(1 << 24, 1, 0, 1, 1, {"max_pass_len": 4096})
     assert d["pass_len"][:2] == [4096, 4096] and d["kernel_variant"][:2] == [9, 9], d

@@ -119,6 +119,35 @@ def test_col_unaligned_buffers(cuda, n):
     assert np.array_equal(b, b2)
 
 
+@pytest.mark.parametrize("n,B", [(1 << 14, 3), (1 << 16, 2), (1 << 17, 2), (1 << 18, 2), (1 << 19, 1),
+                                 (1 << 23, 1)])
+def test_col_half_tiles(cuda, oracle, n, B):
+    """FP32 passes of 128 .. 512 run 32 KB tiles by default (half the units
+    of the 64 KB tiles that blocks_per_sm = 1 keeps): against the exact
+    oracle (up to 2^19) and the 64 KB plan, forward and inverse, in and out
+    of place."""
+    from gfft_gb300 import _lib
+    one = {"blocks_per_sm": 1}
+    d1 = _lib.plan_query(n, 1, 0, 1, B, one)
+    d = _lib.plan_query(n, 1, 0, 1, B)
+    P = d["n_global_passes"]
+    assert d["kernel_variant"][:P] == [9] * P, d
+    for g in range(P):
+        if 128 <= d["pass_len"][g] <= 512:
+            assert 2 * d["units"][g] == d1["units"][g] and d["threads"][g] == 256, (d, d1)
+    x = inputs.gaussian(41 + n + B, 2 * n * B).astype(np.float32)
+    for tr in (0, 1):
+        y = run(cuda, n, 1, tr, 1, x, batch=B)
+        ref = run(cuda, n, 1, tr, 1, x, batch=B, opts=one)
+        assert rel(y, ref) <= tol(n, 0), (n, tr, rel(y, ref))
+        inp = run(cuda, n, 1, tr, 0, x, batch=B)
+        assert np.array_equal(y, inp), (n, tr)
+        if n > 1 << 19:
+            continue
+        ex = oracle.fft_ld(x.astype(np.float64), n, B, 1 if tr == 0 else -1)
+        assert rel(y, ex) <= tol(n, 0), (n, tr, rel(y, ex))
+
+
 REAL = [(1 << 19, 1, 2, 0), (1 << 19, 1, 3, 1), (1 << 13, 1, 3, 1), (1 << 14, 0, 2, 1), (1 << 16, 0, 2, 0),
         (1 << 17, 1, 1, 1), (1 << 20, 0, 1, 1), (1 << 21, 0, 1, 1), (1 << 23, 0, 1, 1)]
 

@@ -27,9 +27,9 @@ def test_mlp_forward_and_gradients_match_reference(cuda):
 
 def test_mlp_training_fits_smooth_target(cuda):
     rng = np.random.default_rng(2)
-    X = rng.uniform(-1, 1, size=(1500, 24)).astype(np.float32)
-    y = (np.sin(2 * X[:, 0]) + 0.5 * X[:, 1] * X[:, 2]).astype(np.float32)
     m = tuner.MLP(seed=3)
+    X = rng.uniform(-1, 1, size=(1500, m.nin)).astype(np.float32)
+    y = (np.sin(2 * X[:, 0]) + 0.5 * X[:, 1] * X[:, 2]).astype(np.float32)
     l0 = float(np.mean((m.predict(X) - y) ** 2))
     l1 = m.train(X, y, epochs=1500, lr=3e-3)
     assert l1 < 0.1 * l0 and l1 < 0.02, (l0, l1)

@@ -1,6 +1,7 @@
 """CPU: tuner candidate enumeration and plan features (no GPU), and the FP64
 reference of the cost model pinned by finite differences."""
 import numpy as np
+import pytest
 
 from gfft_gb300 import _lib
 from gfft_gb300 import tuner
@@ -60,3 +61,16 @@ def test_mlp_reference_gradients_finite_difference():
         e[i] = 1e-6
         fd = (loss(p + e) - loss(p - e)) / 2e-6
         assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])
+
+
+def test_mlp_rejects_rows_of_the_wrong_width():
+    """The library reads len(X) * nin features: a matrix of another width is
+    refused on the host before any copy."""
+    m = tuner.MLP.__new__(tuner.MLP)  # no device state: only the host-side check
+    m.nin = 25
+    with pytest.raises(ValueError):
+        m._rows(np.zeros((3, 24), dtype=np.float32))
+    with pytest.raises(ValueError):
+        m._rows(np.zeros((3, 25), dtype=np.float32), np.zeros(4, dtype=np.float32))
+    X, y = m._rows(np.zeros((3, 25)), np.zeros(3))
+    assert X.dtype == np.float32 and X.flags.c_contiguous and y.shape == (3,)
