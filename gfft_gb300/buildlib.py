@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
               "-I" + CSRC, "-I" + INCLUDE] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-I" + CSRC, "-I" + INCLUDE]
 
-CUDA_SOURCES = ["fft_engine.cu", "fft_fast.cu", "fft_spec.cu", "fft_lane.cu", "fft_tc.cu", "fft_mixed.cu", "fft_col.cu", "fft_col_real.cu", "gfft_capi.cu", "gfft_dct.cu", "gfft_nd.cu", "gfft_noalloc.cu", "gfft_ragged.cu", "gfft_tune.cu", "gfft_peak.cu"]
+CUDA_SOURCES = ["fft_engine.cu", "fft_fast.cu", "fft_spec.cu", "fft_lane.cu", "fft_tc.cu", "fft_mixed.cu", "fft_col.cu", "fft_col_real.cu", "fft_colmix.cu", "gfft_capi.cu", "gfft_dct.cu", "gfft_nd.cu", "gfft_noalloc.cu", "gfft_ragged.cu", "gfft_tune.cu", "gfft_peak.cu"]
 CXX_SOURCES = ["planner.cpp", "colshape.cpp", "capi_host.cpp"]
 
 

@@ -52,12 +52,12 @@ constexpr int work_bytes_rf(int esz, int L, int rf, int tk = 64) {
 }
 // pass lengths with a kernel: powers of two 64 .. 4096 (FP32) / 2048 (FP64);
 // real-pair tiles need two units of each kind (W >= 4 for FP32: an even first
-// column of region A); 32 KB tiles for FP32 complex passes of 128 .. 512
-// (rows of 64 bytes or more)
+// column of region A); 32 KB tiles for FP32 complex passes of 128 .. 1024
+// (rows of 32 bytes or more)
 constexpr bool supported(int esz, int L, int rf, int tk = 64) {
   return L >= 64 && (L & (L - 1)) == 0 && L <= (esz == 16 ? 2048 : 4096) &&
          (!rf || (L <= 2048 && (esz == 16 ? lanes(esz, L) >= 2 : lanes(esz, L) >= 4))) &&
-         (tk == 64 || (tk == 32 && esz == 8 && !rf && L >= 128 && L <= 512));
+         (tk == 64 || (tk == 32 && esz == 8 && !rf && L >= 128 && L <= 1024));
 }
 // in-block twiddles of a pass, sum over its in-block passes of (R - 1) Ns
 // = L - 1 (the product telescopes): the contiguous block of the plan's table
@@ -68,6 +68,40 @@ constexpr int tw_bytes(int esz, int L) { return ((tw_entries(L) * esz + 15) / 16
 // buffer, the in-block twiddles and one mbarrier per stage
 constexpr long long smem_bytes(int esz, int L, int rf, int stages, int tk = 64) {
   return (long long)stages * stage_bytes(esz, L, rf, tk) + work_bytes_rf(esz, L, rf, tk) + tw_bytes(esz, L) +
+         8LL * stages;
+}
+
+// ---- mixed-radix passes (L not a power of two, colmix.cuh) ----
+// units per tile: the largest power of two W <= 64 with W L esz <= 64 KB
+// (at least 2)
+constexpr int mix_lanes(int esz, int L) {
+  int w = 2;
+  while (w < 64 && 2LL * w * L * esz <= 65536) w *= 2;
+  return w;
+}
+// rows per tensor box: the largest divisor of L that is at most 256
+constexpr int mix_rows(int L) {
+  int b = L < 256 ? L : 256;
+  while (L % b) --b;
+  return b;
+}
+// padded element index and lane stride of the work buffers: one slot per
+// 2^ps elements and one more per 2^(ps+4) (strides of 2^(ps+4) elements
+// would otherwise fall on one bank), odd lane stride
+constexpr int mix_pad(int esz, int s) { return s + (s >> ps(esz)) + (s >> (ps(esz) + 4)); }
+constexpr int mix_stride(int esz, int L) { return (mix_pad(esz, L) + 1) | 1; }
+constexpr int mix_threads() { return 512; }
+constexpr int mix_stage_bytes(int esz, int L) { return round1k(mix_lanes(esz, L) * L * esz); }
+constexpr int mix_work_bytes(int esz, int L) { return round1k(mix_lanes(esz, L) * mix_stride(esz, L) * esz); }
+constexpr int mix_tw_bytes(int esz, int L) { return ((L - 1) * esz + 15) / 16 * 16; }
+// tensor boxes start on 128-byte boundaries of the stage (and of the dense
+// tile a later pass stores from)
+constexpr bool mix_supported(int esz, int L) {
+  return L >= 64 && (L & (L - 1)) != 0 && (mix_rows(L) * mix_lanes(esz, L) * esz) % 128 == 0;
+}
+// stages, two work buffers, the in-block twiddles, one mbarrier per stage
+constexpr long long mix_smem_bytes(int esz, int L, int stages) {
+  return (long long)stages * mix_stage_bytes(esz, L) + 2LL * mix_work_bytes(esz, L) + mix_tw_bytes(esz, L) +
          8LL * stages;
 }
 

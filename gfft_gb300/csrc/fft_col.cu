@@ -49,12 +49,13 @@ int encode(CUtensorMap* m, const void* base, long long rows, long long cols, int
 
 template <typename T>
 const void* col_fn(int L, int tk) {
-  if (tk == 32) {  // half-size tiles: FP32 passes of 128 .. 512
+  if (tk == 32) {  // half-size tiles: FP32 passes of 128 .. 1024
     if (sizeof(T) != 4) return nullptr;
     switch (L) {
       case 128: return (const void*)gfft::col_kernel<float, 128, 0, 32>;
       case 256: return (const void*)gfft::col_kernel<float, 256, 0, 32>;
       case 512: return (const void*)gfft::col_kernel<float, 512, 0, 32>;
+      case 1024: return (const void*)gfft::col_kernel<float, 1024, 0, 32>;
       default: return nullptr;
     }
   }
@@ -75,6 +76,13 @@ const void* kernel_of(int dbl, int L, int rf, int tk) {
   return dbl ? col_fn<double>(L, tk) : col_fn<float>(L, tk);
 }
 }  // namespace
+
+// a 2-D tensor map (fft_colmix.cu): rows x cols elements of esz bytes at
+// base, boxes of w x br elements; 0 on success
+extern "C" int gfft_tmap_2d(void* map, const void* base, long long rows, long long cols, int esz, int w, int br) {
+  if (get_encoder() != 0) return 1;
+  return encode(reinterpret_cast<CUtensorMap*>(map), base, rows, cols, esz, w, br);
+}
 
 extern "C" int gfft_col_setup(int dbl, size_t max_smem) {
   if (get_encoder() != 0) return 1;

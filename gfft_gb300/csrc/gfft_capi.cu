@@ -53,6 +53,10 @@ extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, int tk, unsigned gr
                                cudaStream_t stream);
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
+extern "C" int gfft_colmix_setup(int dbl, size_t max_smem);
+extern "C" int gfft_colmix_occupancy(int dbl, const EngineArgs* a, int threads, size_t smem);
+extern "C" int gfft_colmix_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
+                                  cudaStream_t stream);
 
 
 namespace {
@@ -78,6 +82,7 @@ int setup_device_once(int dbl) {
   if (!dbl && gfft_tc_setup((size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_mixed_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (gfft_col_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
+  if (gfft_colmix_setup(dbl, (size_t)maxopt) != 0) return GFFT_E_CUDA;
   if (dev < 64) done[dbl][dev] = true;
   return GFFT_OK;
 }
@@ -93,6 +98,17 @@ int mixed_occupancy(int dbl, const GlobalPass& gp) {
   a.npass = gp.npass;
   for (int i = 0; i < gp.npass; ++i) a.pass[i] = gp.pass[i];
   return gfft_mixed_occupancy(dbl, &a, gp.threads, gp.smem);
+}
+
+// occupancy of a tensor-copy pass (power-of-two length, or a mixed shape)
+int col_occupancy(int dbl, const GlobalPass& gp) {
+  if ((gp.L & (gp.L - 1)) == 0) return gfft_col_occupancy(dbl, gp.L, gp.rf, gp.tk, gp.threads, gp.smem);
+  EngineArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.L = gp.L;
+  a.npass = gp.npass;
+  for (int i = 0; i < gp.npass; ++i) a.pass[i] = gp.pass[i];
+  return gfft_colmix_occupancy(dbl, &a, gp.threads, gp.smem);
 }
 
 }  // namespace
@@ -180,7 +196,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)
                        : gp.variant == 7 ? mixed_occupancy(dbl, gp)
-                       : gp.variant == 9 ? gfft_col_occupancy(dbl, gp.L, gp.rf, gp.tk, gp.threads, gp.smem)
+                       : gp.variant == 9 ? col_occupancy(dbl, gp)
                                          : gfft_fast_occupancy(dbl, gp.threads, gp.smem));
       if (gp.variant == 6 && !(opts && opts->blocks_per_sm)) {
         // two blocks fit by registers (launch bound) and shared memory whenever
@@ -404,8 +420,10 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
       a.ntiles = gp.ntiles;
       a.stages = gp.stages;
       a.spin_limit = 1LL << 26;
-      if (gfft_col_launch(dbl, &a, gp.tk, h->grid[g], (unsigned)gp.threads, gp.smem, stream) != 0)
-        return GFFT_E_CUDA;
+      const int e = (gp.L & (gp.L - 1)) == 0
+                        ? gfft_col_launch(dbl, &a, gp.tk, h->grid[g], (unsigned)gp.threads, gp.smem, stream)
+                        : gfft_colmix_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream);
+      if (e != 0) return GFFT_E_CUDA;
       continue;
     }
     if (gp.variant == 7) {

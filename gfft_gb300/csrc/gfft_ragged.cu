@@ -84,6 +84,43 @@ __device__ __noinline__ typename Vec<T>::t* ct_passes(typename Vec<T>::t* b0, ty
   return b0;
 }
 
+// Warm L2 with the input tile of work item `it` (issued before the current
+// item's passes, so that its load later hits L2 instead of waiting on
+// DRAM): one prefetch per 128-byte line of each row segment of a column
+// tile, or of each gathered transform of a single-pass group.  The lines
+// are the ones load_tile reads; a later pass's input may still be in
+// flight from its earlier pass, in which case the line is fetched again
+// when written (L2 is the point of coherence), so the hint is only ever
+// early, never stale data.
+__device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+template <typename T>
+__device__ __forceinline__ void prefetch_item(const RaggedArgs& ra, long long it) {
+  typedef typename Vec<T>::t V;
+  const RaggedItem item = ra.items[it];
+  const RaggedPlan& pl = ra.plans[item.plan];
+  constexpr int ESZ = (int)sizeof(V);
+  if (pl.nglobal == 1) {
+    const long long L = pl.n;
+    const int lines = (int)((L * ESZ + 127) / 128);
+    for (int i = threadIdx.x; i < item.count * lines; i += blockDim.x) {
+      const int l = i / lines, c = i - l * lines;
+      pf_l2((const char*)ra.in + ra.lane_off[item.group + l] * ESZ + (long long)c * 128);
+    }
+  } else {
+    const int g = item.pass;
+    const V* base = g == 0 ? (const V*)ra.in : (const V*)ra.ws + (g == 2 ? ra.ws2_off : 0);
+    base += ra.offset[item.transform] + item.unit0;
+    const int L = pl.L[g];
+    const long long stride = pl.n / L;
+    const int seg = (item.count * ESZ + 127) / 128;  // lines per row segment
+    for (int i = threadIdx.x; i < L * seg; i += blockDim.x) {
+      const int s = i / seg, c = i - s * seg;
+      pf_l2((const char*)(base + (long long)s * stride) + c * 128);
+    }
+  }
+}
+
 // resident blocks per SM the register budget is sized for (70 KB of shared
 // memory per block)
 template <typename T> struct RaggedOcc { static constexpr int v = sizeof(T) == 4 ? 3 : 2; };
@@ -157,9 +194,11 @@ __global__ void __launch_bounds__(256, RaggedOcc<T>::v) ragged_kernel(const __gr
     // passes (the value is used only after them).  A block never holds a
     // claim on an item listed before the one it works on, so the dependency
     // waits still always end.
-    long long next_item = 0;
-    if (threadIdx.x == 0) next_item = atomicAdd(ra.head, 1);
+    __shared__ long long next_s;
+    if (threadIdx.x == 0) next_s = atomicAdd(ra.head, 1);
     __syncthreads();
+    const long long next_item = next_s;
+    if (next_item < ra.nitems) prefetch_item<T>(ra, next_item);
     V* src = b0;
     V* dst = b1;
     const V* tw = (const V*)ea.tw;

@@ -62,8 +62,10 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   ks.push_back({0, 0, 16, 0, 0, 0});
   for (int st : {1, 2, 3})
     if (st != dflt_st) ks.push_back({0, 0, 16, 0, st, 0});
-  // 64 KB tensor-copy tiles where FP32 passes of 128 .. 512 default to 32 KB
+  // 64 KB tensor-copy tiles where FP32 passes of 128 .. 512 default to 32 KB,
+  // and 32 KB tiles on FP32 passes of 1024 too
   for (int cap : {0, 4096, 1024}) ks.push_back({cap, 0, 16, 0, 0, 0, 1});
+  for (int cap : {0, 4096}) ks.push_back({cap, 0, 16, 0, 0, 0, 2});
   // wider column tiles (128- and 256-byte rows) with shorter passes
   for (int cap : {0, 512, 256, 128})
     for (int w : {16, 32}) ks.push_back({cap, 0, 16, 0, 0, w});

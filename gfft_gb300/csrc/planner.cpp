@@ -28,6 +28,8 @@
 bool spec_radices(const GlobalPass& gp);
 // fft_col.cu: launch shape of the tensor-copy column tiles (variant 9)
 extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int tk, int* units, int* threads, size_t* smem);
+extern "C" int gfft_colmix_shape(int dbl, int L, const int* rs, int np, int stages, int* units, int* threads,
+                                 size_t* smem);
 
 namespace {
 
@@ -428,6 +430,27 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.ntiles = (batch * stride + W - 1) / W;
         // two gathered tiles and the work buffer, padded as fft_mixed.cu padded_len
         gp.smem = (size_t)(3 * W * epadded(gp.L) * esz);
+        // the same shape moved by 2-D tensor copies (fft_colmix.cu, variant
+        // 9) where every tile of W units lies in one transform and one output
+        // box (W divides N / L and Ns) and the row pitches are multiples of
+        // 16 bytes; two stages where they fit the shared memory
+        int mW = 0, mT = 0;
+        size_t msm = 0;
+        int S = o.stages > 0 ? o.stages : 2;
+        if (col_ok && plan.nglobal > 1 && gfft_colmix_shape(dbl, gp.L, rs, gp.npass, S, &mW, &mT, &msm) == 0 &&
+            stride % mW == 0 && (g == 0 || Ns % mW == 0) && (stride * esz) % 16 == 0 &&
+            (g == 0 || (Ns * esz) % 16 == 0)) {
+          while (S > 1 && msm > 227 * 1024) gfft_colmix_shape(dbl, gp.L, rs, gp.npass, --S, &mW, &mT, &msm);
+          if (msm <= 227 * 1024) {
+            gp.variant = 9;
+            gp.units = mW;
+            gp.threads = mT;
+            gp.stages = S;
+            gp.tk = 64;
+            gp.smem = msm;
+            gp.ntiles = batch * stride / mW;
+          }
+        }
       }
     }
     // split-precision tensor-core form, on request: FP32 complex, power-of-two
@@ -457,7 +480,8 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       // stages 2-12 % faster for passes of 128 .. 2048 with 64 KB tiles,
       // within 2 % for 1024 x 1024).
       int tk = 64;
-      if (o.bps != 1 && gfft_col_shape(dbl, gp.L, 1, 0, 32, &W, &T, &sm) == 0) tk = 32;
+      if (o.bps != 1 && (gp.L <= 512 || o.bps == 2) && gfft_col_shape(dbl, gp.L, 1, 0, 32, &W, &T, &sm) == 0)
+        tk = 32;  // (FP32 passes of 1024: 32-byte rows, on request only)
       int S = o.stages > 0 ? o.stages : (tk == 32 ? 1 : 2);
       if (gfft_col_shape(dbl, gp.L, S, 0, tk, &W, &T, &sm) == 0 && (n / gp.L) % W == 0 && (g == 0 || Ns % W == 0)) {
         while (S > 1 && sm > 227 * 1024) gfft_col_shape(dbl, gp.L, --S, 0, tk, &W, &T, &sm);
@@ -549,10 +573,11 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       }
     }
   }
-  // variant-9 later passes: W_(16 Ns)^(k r), r < 16, k < Ns, when at most 2^20 entries
+  // variant-9 later passes of power-of-two length: W_(16 Ns)^(k r), r < 16,
+  // k < Ns, when at most 2^20 entries
   for (int g = 1; g < plan.nglobal; ++g) {
     const GlobalPass& gp = plan.gp[g];
-    if (gp.variant == 9 && 16 * gp.Ns <= (1LL << 20)) {
+    if (gp.variant == 9 && (gp.L & (gp.L - 1)) == 0 && 16 * gp.Ns <= (1LL << 20)) {
       plan.ftw_off[g] = off;
       off += (std::size_t)(16 * gp.Ns);
     }

@@ -100,7 +100,8 @@ typedef struct gfft_plan_opts {
   int stages;             /* bulk-copy pipeline depth of the fast path (0 = 2) */
   int blocks_per_sm;      /* persistent blocks per SM of the fast path (0 = occupancy); for the
                              tensor-copy column tiles, 1 keeps 64 KB tiles on FP32 passes of
-                             128..512 (default there: 32 KB tiles, one stage, two blocks per SM) */
+                             128..512 (default there: 32 KB tiles, one stage, two blocks per SM)
+                             and 2 extends the 32 KB tiles to FP32 passes of 1024 */
   int decimation;         /* 0 = in time (DIT, default), 1 = in frequency (DIF: the transposed
                              Stockham passes in reverse order, twiddles after the butterflies;
                              the reference's InFreq / T_DFTk_x_Im, src/gfftalgfreq.h:106-432);

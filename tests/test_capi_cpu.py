@@ -121,7 +121,11 @@ def test_plan_column_kernel_selection():
 
 def test_plan_mixed_kernel_selection():
     """Mixed-radix pass shapes with a compile-time kernel take variant 7."""
-    assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8)["kernel_variant"] == [9, 7]  # power-of-two pass on variant 9
+    # the 768-point pass too: mixed shapes move by tensor copies where W divides N / L and Ns
+    assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8)["kernel_variant"] == [9, 9]
+    assert _lib.plan_query(2 ** 10 * 3 ** 5, 1, 0, 1, 8)["kernel_variant"] == [9, 9]
+    assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8, {"kernel_variant": 7})["kernel_variant"][1] == 7
+    assert _lib.plan_query(360 * 360, 1, 0, 1, 8)["kernel_variant"] == [7, 7]  # 16 units do not divide 360
     assert _lib.plan_query(5 ** 8, 0, 0, 1, 8)["kernel_variant"] == [7, 7]
     assert _lib.plan_query(768, 1, 0, 1, 100)["kernel_variant"] == [7]
     assert _lib.plan_query(768, 1, 0, 1, 100, {"kernel_variant": 1})["kernel_variant"] == [1]

@@ -148,6 +148,29 @@ def test_col_half_tiles(cuda, oracle, n, B):
         assert rel(y, ex) <= tol(n, 0), (n, tr, rel(y, ex))
 
 
+@pytest.mark.parametrize("n,B", [(1 << 19, 2), (1 << 20, 1), (1 << 21, 1)])
+def test_col_half_tiles_1024(cuda, oracle, n, B):
+    """blocks_per_sm = 2 extends the 32 KB tiles to FP32 passes of 1024 (4
+    units, 32-byte rows): against the default plan and, up to 2^20, the
+    exact oracle, forward and inverse."""
+    from gfft_gb300 import _lib
+    two = {"blocks_per_sm": 2}
+    d = _lib.plan_query(n, 1, 0, 1, B, two)
+    P = d["n_global_passes"]
+    assert 1024 in d["pass_len"][:P], d
+    for g in range(P):
+        if d["pass_len"][g] == 1024:
+            assert d["units"][g] == 4 and d["threads"][g] == 256, d
+    x = inputs.gaussian(43 + n + B, 2 * n * B).astype(np.float32)
+    for tr in (0, 1):
+        y = run(cuda, n, 1, tr, 1, x, batch=B, opts=two)
+        ref = run(cuda, n, 1, tr, 1, x, batch=B)
+        assert rel(y, ref) <= tol(n, 0), (n, tr, rel(y, ref))
+        if n <= 1 << 20:
+            ex = oracle.fft_ld(x.astype(np.float64), n, B, 1 if tr == 0 else -1)
+            assert rel(y, ex) <= tol(n, 0), (n, tr, rel(y, ex))
+
+
 REAL = [(1 << 19, 1, 2, 0), (1 << 19, 1, 3, 1), (1 << 13, 1, 3, 1), (1 << 14, 0, 2, 1), (1 << 16, 0, 2, 0),
         (1 << 17, 1, 1, 1), (1 << 20, 0, 1, 1), (1 << 21, 0, 1, 1), (1 << 23, 0, 1, 1)]
 

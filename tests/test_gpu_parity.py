@@ -455,18 +455,50 @@ def test_mixed_columns(cuda, oracle, n, B, dbl):
     from gfft_gb300 import _lib
     vt = 0 if dbl else 1
     dt = np.float64 if dbl else np.float32
-    assert 7 in _lib.plan_query(n, vt, 0, 1, B)["kernel_variant"]
+    v7 = {"kernel_variant": 7}
+    assert 7 in _lib.plan_query(n, vt, 0, 1, B, v7)["kernel_variant"]
     x = inputs.gaussian(23 + n, 2 * n * B).astype(dt)
     for tr in (0, 1):
-        y = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+        y = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts=v7)
         gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
         assert rel(y, gen) <= tol(n, dbl), (n, tr, rel(y, gen))
-        yi = run_gpu(cuda, n, vt, tr, 0, x, batch=B)
+        yi = run_gpu(cuda, n, vt, tr, 0, x, batch=B, opts=v7)
         assert np.array_equal(y, yi), (n, tr)
     k = min(B, max(1, (1 << 20) // n))
     ex = oracle.fft_ld(x[:2 * n * k].astype(np.float64), n, k, 1)
-    y = run_gpu(cuda, n, vt, 0, 1, x[:2 * n * k], batch=k)
+    y = run_gpu(cuda, n, vt, 0, 1, x[:2 * n * k], batch=k, opts=v7)
     assert rel(y, ex) <= tol(n, dbl), (n, rel(y, ex))
+
+
+@pytest.mark.parametrize("dbl", [0, 1])
+@pytest.mark.parametrize("n,B", [(3 * 2 ** 18, 3), (2 ** 10 * 3 ** 5, 3), (1000 * 1000, 1), (480 * 1024, 2),
+                                 (768 * 768, 1), (432 * 432, 2), (576 * 576, 1), (480 * 480, 2), (360 * 360, 2)])
+def test_mixed_tensor_copy_columns(cuda, oracle, n, B, dbl):
+    """Mixed-radix passes moved by 2-D tensor copies (variant 9 with a pass
+    length that is not a power of two), the default where W divides N / L
+    and Ns: against the copy-free mixed tiles (variant 7), the generic engine
+    and, up to 2^20 points, the exact oracle; forward and inverse, in and out
+    of place."""
+    from gfft_gb300 import _lib
+    vt = 0 if dbl else 1
+    dt = np.float64 if dbl else np.float32
+    d = _lib.plan_query(n, vt, 0, 1, B)
+    P = d["n_global_passes"]
+    mixed9 = [g for g in range(P) if d["kernel_variant"][g] == 9 and d["pass_len"][g] & (d["pass_len"][g] - 1)]
+    if (n, dbl) != (360 * 360, 0):  # FP32 360: 16 units do not divide 360 (variant 7 stays)
+        assert mixed9, d
+    x = inputs.gaussian(31 + n + B, 2 * n * B).astype(dt)
+    for tr in (0, 1):
+        y = run_gpu(cuda, n, vt, tr, 1, x, batch=B)
+        v7 = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 7})
+        gen = run_gpu(cuda, n, vt, tr, 1, x, batch=B, opts={"kernel_variant": 1})
+        assert rel(y, v7) <= tol(n, dbl), (n, tr, rel(y, v7))
+        assert rel(y, gen) <= tol(n, dbl), (n, tr, rel(y, gen))
+        yi = run_gpu(cuda, n, vt, tr, 0, x, batch=B)
+        assert np.array_equal(y, yi), (n, tr)
+        if n * B <= 1 << 20:
+            ex = oracle.fft_ld(x.astype(np.float64), n, B, 1 if tr == 0 else -1)
+            assert rel(y, ex) <= tol(n, dbl), (n, tr, rel(y, ex))
 
 
 @pytest.mark.parametrize("n,dbl,B,cap", [(1 << 13, 0, 3, 1024), (1 << 16, 0, 2, 0), (1 << 20, 0, 1, 0),
