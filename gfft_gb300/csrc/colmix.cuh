@@ -10,7 +10,8 @@
 // radices need not divide 16:
 //  - first pass (radix R0) from the dense stage, lane-fastest (a warp reads
 //    consecutive words of a stage row), with the conjugation of the inverse
-//    and the four-step twiddle W_N^(k s N/(Ns L)) applied on load, written
+//    and the four-step twiddle W_N^(k s N/(Ns L)) applied on load (factored
+//    as in col.cuh, with a [R0][Ns] table of W_(R0 Ns)^(k r)), written
 //    to a padded [lane][Lp] work buffer; the stage is then free for the copy
 //    of the tile S tiles ahead;
 //  - the middle passes ping-pong between two padded work buffers, one
@@ -180,7 +181,15 @@ __global__ void __launch_bounds__(colshape::mix_threads(), 1)
         if (!a.notw) {
           const unsigned k = (unsigned)((p * W + lane) % gNs);
           const unsigned kstep = k * kfac;
-          if (kstep) {
+          if (kstep && a.ftw) {
+            // W_N^(kstep (j + r NB0)) = W_N^(kstep j) * W_(R0 Ns)^(k r): one
+            // lookup of the first factor, the second from the [r][k] table
+            const unsigned m0 = kstep * (unsigned)j;  // < N < 2^32
+            const V t0 = cmul(__ldg(lo + (m0 & mask)), __ldg(hi + (m0 >> lgB)));
+            const V* t2 = (const V*)a.ftw + k;
+#pragma unroll
+            for (int r = 0; r < R0; ++r) v[r] = cmul(v[r], cmul(t0, __ldg(t2 + (size_t)r * gNs)));
+          } else if (kstep) {
 #pragma unroll
             for (int r = 0; r < R0; ++r) {
               const unsigned m = kstep * (unsigned)(j + r * NB0);  // < N < 2^32
@@ -270,6 +279,181 @@ __global__ void __launch_bounds__(colshape::mix_threads(), 1)
     // reads of the work buffers before its first writes
   }
   if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+
+// The same passes with the tile gathered by 8 / 16-byte cp.async copies (one
+// per element) instead of tensor copies, and the outputs stored from
+// registers: for passes whose tiles do not fit the tensor maps (W does not
+// divide N / L or Ns, or a row pitch is not a multiple of 16 bytes, as for
+// N = 5^8 = 625 x 625).  A tile's W lanes are units u = tile W + lane of the
+// whole batch, each with its own transform and column, so a tile may span
+// transforms and the last one may be partial.  S = 1 or 2 stages, each
+// thread waiting on its own copies (cp.async.wait_group) before a barrier.
+template <typename T, int R0, int R1, int R2, int R3>
+__global__ void __launch_bounds__(colshape::mix_threads(), 1) colmix_gather_kernel(const __grid_constant__ EngineArgs a) {
+  using namespace colmix;
+  typedef MixShape<T, R0, R1, R2, R3> Sh;
+  typedef typename Vec<T>::t V;
+  constexpr int L = Sh::L, W = Sh::W, NT = Sh::NT, LP = Sh::LP, NP = Sh::NP, TB = Sh::TB;
+  constexpr int RL = NP == 4 ? R3 : (NP == 3 ? R2 : (NP == 2 ? R1 : R0));
+  constexpr int NSL = L / RL;
+  static_assert(NP >= 2, "a mixed shape has two or more in-block passes");
+  static_assert(NT % W == 0, "each thread keeps one lane");
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ long long lane_t[W], lane_b[W];  // transform and unit of each lane of the current tile
+  const int S = a.stages;  // 1 or 2
+  V* const w0 = reinterpret_cast<V*>(smem + (size_t)S * TB);
+  V* const w1 = reinterpret_cast<V*>(smem + (size_t)S * TB + Sh::WB);
+  V* const stw = reinterpret_cast<V*>(smem + (size_t)S * TB + 2 * (size_t)Sh::WB);
+  const int tw0 = a.pass[0].tw;
+  for (int e = threadIdx.x; e < L - 1; e += NT) stw[e] = __ldg((const V*)a.tw + tw0 + e);
+  const T sc = (T)a.scale;
+  const bool conj = a.conj != 0;
+  const long long G = gridDim.x;
+  const long long stride = a.stride;
+  const long long gNs = a.gNs;
+  const unsigned kfac = (unsigned)(a.N / (gNs * L));
+  const V* lo = (const V*)a.gtw_lo;
+  const V* hi = (const V*)a.gtw_hi;
+  const unsigned mask = (unsigned)a.gB - 1;
+  const int lgB = 31 - __clz((int)a.gB);
+  const int my_lane = threadIdx.x % W;  // the lane this thread gathers, twiddles and stores
+
+  // every thread copies its lane's rows of tile `tile` into stage s (zeros
+  // past the last unit), then closes its copy group (empty past the end)
+  auto gather = [&](long long tile, int s) {
+    V* st = reinterpret_cast<V*>(smem + (size_t)s * TB);
+    if (tile < a.ntiles) {
+      const long long u = tile * W + my_lane;
+      if (u < a.nunits) {
+        const long long t = u / stride, b = u - t * stride;
+        const V* src = (const V*)a.in + t * a.N + b;
+        for (int row = threadIdx.x / W; row < L; row += NT / W)
+          lanep2::cpa<T>(lanep2::sa(st + row * W + my_lane), src + (long long)row * stride);
+      } else {
+        for (int row = threadIdx.x / W; row < L; row += NT / W) st[row * W + my_lane] = mk<V>(0, 0);
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  for (int s = 0; s < S; ++s) gather(blockIdx.x + (long long)s * G, s);
+
+  int it = 0;
+  for (long long tile = blockIdx.x; tile < a.ntiles; tile += G, ++it) {
+    const int s = it % S;
+    if (S == 2)
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (threadIdx.x < W) {
+      const long long u = tile * W + threadIdx.x;
+      const long long t = u / stride;
+      lane_t[threadIdx.x] = t;
+      lane_b[threadIdx.x] = u - t * stride;
+    }
+    __syncthreads();  // stage s complete (every thread's copies), lane table written
+    const V* const stg = reinterpret_cast<const V*>(smem + (size_t)s * TB);
+    const long long my_u = tile * W + my_lane;
+    const long long my_b = lane_b[my_lane], my_t = lane_t[my_lane];
+
+    // first pass (radix R0) from the dense stage, lane-fastest
+    {
+      constexpr int NB0 = L / R0;
+      const unsigned k = (unsigned)(my_b % gNs);
+      const unsigned kstep = a.notw ? 0u : k * kfac;
+      for (int i = threadIdx.x; i < W * NB0; i += NT) {
+        const int j = i / W;
+        V v[R0];
+#pragma unroll
+        for (int r = 0; r < R0; ++r) {
+          const int e = (j + r * NB0) * W + my_lane;
+          if (GFFT_DCHECK(e < W * L, a.status)) v[r] = stg[e];
+        }
+        if (conj)
+#pragma unroll
+          for (int r = 0; r < R0; ++r) v[r] = cconj(v[r]);
+        if (kstep && a.ftw) {
+          const unsigned m0 = kstep * (unsigned)j;  // < N < 2^32
+          const V t0 = cmul(__ldg(lo + (m0 & mask)), __ldg(hi + (m0 >> lgB)));
+          const V* t2 = (const V*)a.ftw + k;
+#pragma unroll
+          for (int r = 0; r < R0; ++r) v[r] = cmul(v[r], cmul(t0, __ldg(t2 + (size_t)r * gNs)));
+        } else if (kstep) {
+#pragma unroll
+          for (int r = 0; r < R0; ++r) {
+            const unsigned m = kstep * (unsigned)(j + r * NB0);  // < N < 2^32
+            v[r] = cmul(v[r], cmul(__ldg(lo + (m & mask)), __ldg(hi + (m >> lgB))));
+          }
+        }
+        dft<T, V, R0>(v);
+        V* d = w0 + my_lane * LP;
+#pragma unroll
+        for (int r = 0; r < R0; ++r) d[padi<T>(j * R0 + r)] = v[r];
+      }
+    }
+    __syncthreads();  // every thread has read stage s
+    gather(tile + (long long)S * G, s);
+    const V* src = w0;
+    if constexpr (NP >= 3) {
+      mid<T, L, W, NT, LP, R1, R0>(w0, w1, stw, a.pass[1].tw - tw0, a.status);
+      __syncthreads();
+      src = w1;
+    }
+    if constexpr (NP >= 4) {
+      mid<T, L, W, NT, LP, R2, R0 * R1>(w1, w0, stw, a.pass[2].tw - tw0, a.status);
+      __syncthreads();
+      src = w0;
+    }
+    const int twl = a.pass[NP - 1].tw - tw0;
+    constexpr int NBL = L / RL;
+    if (gNs == 1) {
+      // first global pass: lane-major, each lane's L outputs contiguous
+      for (int i = threadIdx.x; i < W * NBL; i += NT) {
+        const int lane = i / NBL, j = i - lane * NBL;
+        if (tile * W + lane >= a.nunits) continue;
+        const V* sp = src + lane * LP;
+        V v[RL];
+#pragma unroll
+        for (int r = 0; r < RL; ++r) v[r] = sp[padi<T>(j + r * NBL)];
+#pragma unroll
+        for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], stw[twl + j + (r - 1) * NSL]);
+        dft<T, V, RL>(v);
+        const long long e0 = lane_t[lane] * a.N + lane_b[lane] * L + j;
+        V* d = (V*)a.out + e0;
+#pragma unroll
+        for (int r = 0; r < RL; ++r) {
+          V x = v[r];
+          if (conj) x = cconj(x);
+          if (GFFT_DCHECK(e0 + r * NSL < a.nunits * L, a.status)) d[r * NSL] = cscale(x, sc);
+        }
+      }
+    } else if (my_u < a.nunits) {
+      // later global passes: lane-fastest, y[t N + (b - k) L + k + s Ns]
+      const long long k = my_b % gNs;
+      const long long e0 = my_t * a.N + (my_b - k) * L + k;
+      V* d = (V*)a.out + e0;
+      for (int i = threadIdx.x; i < W * NBL; i += NT) {
+        const int j = i / W;
+        const V* sp = src + my_lane * LP;
+        V v[RL];
+#pragma unroll
+        for (int r = 0; r < RL; ++r) v[r] = sp[padi<T>(j + r * NBL)];
+#pragma unroll
+        for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], stw[twl + j + (r - 1) * NSL]);
+        dft<T, V, RL>(v);
+#pragma unroll
+        for (int r = 0; r < RL; ++r) {
+          V x = v[r];
+          if (conj) x = cconj(x);
+          if (GFFT_DCHECK(e0 + (long long)(j + r * NSL) * gNs < a.nunits * L, a.status))
+            d[(long long)(j + r * NSL) * gNs] = cscale(x, sc);
+        }
+      }
+    }
+    __syncthreads();  // the lane table and the work buffers are reused by the next tile
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 }  // namespace gfft

@@ -19,15 +19,16 @@ extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int tk, int* u
   return 0;
 }
 
-// Shape of the mixed-radix tensor-copy pass (colmix.cuh) of length L with
-// radices rs[0..np): units per tile, threads, and the shared memory of
-// `stages` stages; 1 if the shape has no kernel.
-extern "C" int gfft_colmix_shape(int dbl, int L, const int* rs, int np, int stages, int* units, int* threads,
-                                 size_t* smem) {
+// Shape of the mixed-radix pass (colmix.cuh) of length L with radices
+// rs[0..np), moved by tensor copies (gather 0) or cp.async gathers (gather
+// 1, at most two stages): units per tile, threads, and the dynamic shared
+// memory of `stages` stages; 1 if the shape has no such kernel.
+extern "C" int gfft_colmix_shape(int dbl, int L, const int* rs, int np, int stages, int gather, int* units,
+                                 int* threads, size_t* smem) {
   using namespace gfft::colshape;
   const int esz = dbl ? 16 : 8;
-  if (!rs || !units || !threads || !smem || stages < 1 || np > 4) return 1;
-  if (mixed_shape_index(L, rs, np) < 0 || !mix_supported(esz, L)) return 1;
+  if (!rs || !units || !threads || !smem || stages < 1 || np > 4 || (gather && stages > 2)) return 1;
+  if (mixed_shape_index(L, rs, np) < 0 || (!gather && !mix_supported(esz, L))) return 1;
   *units = mix_lanes(esz, L);
   *threads = mix_threads();
   *smem = (size_t)mix_smem_bytes(esz, L, stages);

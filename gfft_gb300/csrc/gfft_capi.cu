@@ -54,9 +54,9 @@ extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, int tk, unsigned gr
 extern "C" int gfft_real_pass_launch(int dbl, void* data, long long n, long long batch, int dir, const void* rtw,
                                      cudaStream_t stream);
 extern "C" int gfft_colmix_setup(int dbl, size_t max_smem);
-extern "C" int gfft_colmix_occupancy(int dbl, const EngineArgs* a, int threads, size_t smem);
-extern "C" int gfft_colmix_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
-                                  cudaStream_t stream);
+extern "C" int gfft_colmix_occupancy(int dbl, const EngineArgs* a, int gather, int threads, size_t smem);
+extern "C" int gfft_colmix_launch(int dbl, const EngineArgs* a, int gather, unsigned grid, unsigned threads,
+                                  size_t smem, cudaStream_t stream);
 
 
 namespace {
@@ -108,7 +108,7 @@ int col_occupancy(int dbl, const GlobalPass& gp) {
   a.L = gp.L;
   a.npass = gp.npass;
   for (int i = 0; i < gp.npass; ++i) a.pass[i] = gp.pass[i];
-  return gfft_colmix_occupancy(dbl, &a, gp.threads, gp.smem);
+  return gfft_colmix_occupancy(dbl, &a, gp.gather, gp.threads, gp.smem);
 }
 
 }  // namespace
@@ -422,7 +422,7 @@ int gfft_exec_ws(gfft_handle h, const void* src, void* dst, cudaStream_t stream,
       a.spin_limit = 1LL << 26;
       const int e = (gp.L & (gp.L - 1)) == 0
                         ? gfft_col_launch(dbl, &a, gp.tk, h->grid[g], (unsigned)gp.threads, gp.smem, stream)
-                        : gfft_colmix_launch(dbl, &a, h->grid[g], (unsigned)gp.threads, gp.smem, stream);
+                        : gfft_colmix_launch(dbl, &a, gp.gather, h->grid[g], (unsigned)gp.threads, gp.smem, stream);
       if (e != 0) return GFFT_E_CUDA;
       continue;
     }
@@ -564,7 +564,7 @@ int gfft_exec(gfft_handle h, const void* src, void* dst, gfft_stream stream) {
   if (h->nd_inner) return gfft_nd_exec(h, src, dst, (cudaStream_t)stream);
   if ((((uintptr_t)src) | ((uintptr_t)dst)) & 15) {
     bool col = false;
-    for (int g = 0; g < h->hp.nglobal; ++g) col = col || h->hp.gp[g].variant == 9;
+    for (int g = 0; g < h->hp.nglobal; ++g) col = col || (h->hp.gp[g].variant == 9 && !h->hp.gp[g].gather);
     if (col) {
       if (!h->unaligned) {
         gfft_plan_opts o;

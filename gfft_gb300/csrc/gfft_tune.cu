@@ -73,6 +73,8 @@ int gfft_tune_candidates(uint64_t n, int vtype_id, int trans_id, int place_id, u
   // ones are the default
   for (int cap : caps) ks.push_back({cap, 4, 16, 0, 0, 0});
   for (int cap : caps) ks.push_back({cap, 5, 16, 0, 0, 0});
+  // the copy-free mixed-radix tiles where the column tiles of variant 9 take mixed shapes
+  for (int cap : caps) ks.push_back({cap, 7, 16, 0, 0, 0});
   for (int cap : caps)
     for (int v : variants)
       for (int mr : radices)

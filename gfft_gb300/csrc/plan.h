@@ -99,7 +99,7 @@ struct EngineArgs {
   const long long* lane_off;  // mode 2: element offset of each lane's transform
   int ldcg;           // read the input through L2 only (data written by other blocks of this launch)
   int notw;           // lane passes without the four-step twiddle (axis transforms of a multi-dimensional array)
-  const void* ftw;    // variant 9, later global passes: W_(16 Ns)^(k r) at [r * Ns + k] (null: two-level lookups)
+  const void* ftw;    // variant 9, later global passes: W_(R0 Ns)^(k r) at [r * Ns + k] (null: two-level lookups)
   int dif;            // generic engine: frequency decimation (transposed passes, twiddles after the butterflies)
   BlockPass pass[GFFT_MAXP];
 };
@@ -117,6 +117,7 @@ struct GlobalPass {
   int stages;     // variant 2: TMA pipeline depth
   int rf = 0;     // variant 9: real pre (2) / post (1) pass fused into this pass
   int tk = 64;    // variant 9: tile KB (64: one block per SM, 32: two)
+  int gather = 0; // variant 9, mixed shape: tiles gathered by cp.async (no tensor maps)
   long long ntiles;
   int tile_bytes;
 };

@@ -23,13 +23,14 @@
 #include <vector>
 
 #include "mixed_shapes.h"
+#include "colshape.h"
 #include "plan.h"
 
 bool spec_radices(const GlobalPass& gp);
 // fft_col.cu: launch shape of the tensor-copy column tiles (variant 9)
 extern "C" int gfft_col_shape(int dbl, int L, int stages, int rf, int tk, int* units, int* threads, size_t* smem);
-extern "C" int gfft_colmix_shape(int dbl, int L, const int* rs, int np, int stages, int* units, int* threads,
-                                 size_t* smem);
+extern "C" int gfft_colmix_shape(int dbl, int L, const int* rs, int np, int stages, int gather, int* units,
+                                 int* threads, size_t* smem);
 
 namespace {
 
@@ -430,25 +431,36 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
         gp.ntiles = (batch * stride + W - 1) / W;
         // two gathered tiles and the work buffer, padded as fft_mixed.cu padded_len
         gp.smem = (size_t)(3 * W * epadded(gp.L) * esz);
-        // the same shape moved by 2-D tensor copies (fft_colmix.cu, variant
-        // 9) where every tile of W units lies in one transform and one output
-        // box (W divides N / L and Ns) and the row pitches are multiples of
-        // 16 bytes; two stages where they fit the shared memory
+        // the same shape as the column tiles of fft_colmix.cu (variant 9):
+        // moved by 2-D tensor copies where every tile of W units lies in one
+        // transform and one output box (W divides N / L and Ns) and the row
+        // pitches are multiples of 16 bytes, else gathered by cp.async (a
+        // tile may then span transforms); two stages where they fit the
+        // shared memory (the gather kernel keeps 1 KB of static shared memory)
         int mW = 0, mT = 0;
         size_t msm = 0;
-        int S = o.stages > 0 ? o.stages : 2;
-        if (col_ok && plan.nglobal > 1 && gfft_colmix_shape(dbl, gp.L, rs, gp.npass, S, &mW, &mT, &msm) == 0 &&
-            stride % mW == 0 && (g == 0 || Ns % mW == 0) && (stride * esz) % 16 == 0 &&
-            (g == 0 || (Ns * esz) % 16 == 0)) {
-          while (S > 1 && msm > 227 * 1024) gfft_colmix_shape(dbl, gp.L, rs, gp.npass, --S, &mW, &mT, &msm);
-          if (msm <= 227 * 1024) {
+        const int tW = gfft::colshape::mix_lanes((int)esz, gp.L);
+        const bool tma = gfft::colshape::mix_supported((int)esz, gp.L) && stride % tW == 0 &&
+                         (g == 0 || Ns % tW == 0) && (stride * esz) % 16 == 0 && (g == 0 || (Ns * esz) % 16 == 0);
+        // (gathers: FP32 only, one stage by default -- measured 1.1-1.4x two
+        // stages at 2^27 points for 5^8, 3^12 and 360^2; FP64, FP64-pipe
+        // bound, keeps the copy-free mixed tiles there)
+        const int gather = tma ? 0 : 1;
+        const size_t lim = (size_t)(227 * 1024 - (gather ? 1024 : 0));
+        int S = o.stages > 0 ? o.stages : (gather ? 1 : 2);
+        if (gather && S > 2) S = 2;
+        if (col_ok && plan.nglobal > 1 && !(gather && dbl) &&
+            gfft_colmix_shape(dbl, gp.L, rs, gp.npass, S, gather, &mW, &mT, &msm) == 0) {
+          while (S > 1 && msm > lim) gfft_colmix_shape(dbl, gp.L, rs, gp.npass, --S, gather, &mW, &mT, &msm);
+          if (msm <= lim) {
             gp.variant = 9;
             gp.units = mW;
             gp.threads = mT;
             gp.stages = S;
             gp.tk = 64;
+            gp.gather = gather;
             gp.smem = msm;
-            gp.ntiles = batch * stride / mW;
+            gp.ntiles = (batch * stride + mW - 1) / mW;
           }
         }
       }
@@ -573,13 +585,13 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       }
     }
   }
-  // variant-9 later passes of power-of-two length: W_(16 Ns)^(k r), r < 16,
-  // k < Ns, when at most 2^20 entries
+  // variant-9 later passes: W_(R0 Ns)^(k r), r < R0 (the first in-block
+  // radix), k < Ns, when at most 2^20 entries
   for (int g = 1; g < plan.nglobal; ++g) {
     const GlobalPass& gp = plan.gp[g];
-    if (gp.variant == 9 && (gp.L & (gp.L - 1)) == 0 && 16 * gp.Ns <= (1LL << 20)) {
+    if (gp.variant == 9 && gp.pass[0].R * gp.Ns <= (1LL << 20)) {
       plan.ftw_off[g] = off;
-      off += (std::size_t)(16 * gp.Ns);
+      off += (std::size_t)(gp.pass[0].R * gp.Ns);
     }
   }
   plan.table_count = off;
@@ -618,11 +630,11 @@ void gfft_plan_tables(const HostPlan& plan, double* tab) {
       wroot(q, 2 * plan.n, &tab[2 * (plan.rtw_off + q)], &tab[2 * (plan.rtw_off + q) + 1]);
   for (int g = 1; g < plan.nglobal; ++g) {
     if (!plan.ftw_off[g]) continue;
-    const long long ns = plan.gp[g].Ns;
-    for (long long r = 0; r < 16; ++r)
+    const long long ns = plan.gp[g].Ns, r0 = plan.gp[g].pass[0].R;
+    for (long long r = 0; r < r0; ++r)
       for (long long k = 0; k < ns; ++k) {
         const std::size_t e = plan.ftw_off[g] + (std::size_t)(r * ns + k);
-        wroot(k * r, 16 * ns, &tab[2 * e], &tab[2 * e + 1]);
+        wroot(k * r, r0 * ns, &tab[2 * e], &tab[2 * e + 1]);
       }
   }
 }

@@ -125,8 +125,12 @@ def test_plan_mixed_kernel_selection():
     assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8)["kernel_variant"] == [9, 9]
     assert _lib.plan_query(2 ** 10 * 3 ** 5, 1, 0, 1, 8)["kernel_variant"] == [9, 9]
     assert _lib.plan_query(3 * 2 ** 18, 1, 0, 1, 8, {"kernel_variant": 7})["kernel_variant"][1] == 7
-    assert _lib.plan_query(360 * 360, 1, 0, 1, 8)["kernel_variant"] == [7, 7]  # 16 units do not divide 360
-    assert _lib.plan_query(5 ** 8, 0, 0, 1, 8)["kernel_variant"] == [7, 7]
+    # tiles that do not fit a tensor map (16 units do not divide 360; 625-element rows are not a
+    # multiple of 16 bytes) are gathered by cp.async, still variant 9; variant 7 on request
+    assert _lib.plan_query(360 * 360, 1, 0, 1, 8)["kernel_variant"] == [9, 9]
+    assert _lib.plan_query(5 ** 8, 1, 0, 1, 8)["kernel_variant"] == [9, 9]
+    assert _lib.plan_query(5 ** 8, 1, 0, 1, 8, {"kernel_variant": 7})["kernel_variant"] == [7, 7]
+    assert _lib.plan_query(5 ** 8, 0, 0, 1, 8)["kernel_variant"] == [7, 7]  # FP64: no gathered tiles
     assert _lib.plan_query(768, 1, 0, 1, 100)["kernel_variant"] == [7]
     assert _lib.plan_query(768, 1, 0, 1, 100, {"kernel_variant": 1})["kernel_variant"] == [1]
     assert 7 not in _lib.plan_query(768, 1, 2, 1, 100)["kernel_variant"]  # real: fused pre/post in the engine

@@ -106,11 +106,12 @@ def test_col_large_fp32(cuda, oracle, n, opts):
     assert rel(back, x) <= 2 * tol(n, 0)
 
 
-@pytest.mark.parametrize("n", [1 << 16, 1 << 22])
+@pytest.mark.parametrize("n", [1 << 16, 1 << 22, 3 * 2 ** 18, 5 ** 8])
 def test_col_unaligned_buffers(cuda, n):
-    """FP32 buffers aligned to one complex element (8 bytes) but not to 16
-    run through the handle's second plan (column tiles of variant 5), with
-    the same result within tolerance, repeatably."""
+    """FP32 buffers aligned to one complex element (8 bytes) but not to 16:
+    plans with tensor copies run through the handle's second plan (column
+    tiles of variant 5 / the engine), gathered mixed-radix tiles (5^8) run
+    as they are; the same result within tolerance, repeatably."""
     x = inputs.gaussian(29 + n, 2 * n).astype(np.float32)
     a = run(cuda, n, 1, 0, 1, x)
     b = run(cuda, n, 1, 0, 1, x, offset=2)

@@ -472,20 +472,23 @@ def test_mixed_columns(cuda, oracle, n, B, dbl):
 
 @pytest.mark.parametrize("dbl", [0, 1])
 @pytest.mark.parametrize("n,B", [(3 * 2 ** 18, 3), (2 ** 10 * 3 ** 5, 3), (1000 * 1000, 1), (480 * 1024, 2),
-                                 (768 * 768, 1), (432 * 432, 2), (576 * 576, 1), (480 * 480, 2), (360 * 360, 2)])
+                                 (768 * 768, 1), (432 * 432, 2), (576 * 576, 1), (480 * 480, 2), (360 * 360, 2),
+                                 (5 ** 8, 3), (3 ** 12, 1)])
 def test_mixed_tensor_copy_columns(cuda, oracle, n, B, dbl):
-    """Mixed-radix passes moved by 2-D tensor copies (variant 9 with a pass
-    length that is not a power of two), the default where W divides N / L
-    and Ns: against the copy-free mixed tiles (variant 7), the generic engine
-    and, up to 2^20 points, the exact oracle; forward and inverse, in and out
-    of place."""
+    """Mixed-radix passes of variant 9 (a pass length that is not a power of
+    two): moved by 2-D tensor copies where W divides N / L and Ns and the
+    rows fit a tensor map, else gathered by cp.async (FP32 360 x 360: 16
+    units do not divide 360; 5^8 and 3^12: odd rows, tiles spanning
+    transforms, a partial last tile); against the copy-free mixed tiles
+    (variant 7), the generic engine and, up to 2^20 points, the exact
+    oracle; forward and inverse, in and out of place."""
     from gfft_gb300 import _lib
     vt = 0 if dbl else 1
     dt = np.float64 if dbl else np.float32
     d = _lib.plan_query(n, vt, 0, 1, B)
     P = d["n_global_passes"]
     mixed9 = [g for g in range(P) if d["kernel_variant"][g] == 9 and d["pass_len"][g] & (d["pass_len"][g] - 1)]
-    if (n, dbl) != (360 * 360, 0):  # FP32 360: 16 units do not divide 360 (variant 7 stays)
+    if not (dbl and n in (5 ** 8, 3 ** 12)):  # FP64 tiles that need gathers stay on variant 7
         assert mixed9, d
     x = inputs.gaussian(31 + n + B, 2 * n * B).astype(dt)
     for tr in (0, 1):
