@@ -45,8 +45,14 @@ __device__ __forceinline__ void ct_pass(const typename Vec<T>::t* __restrict__ s
   typedef typename Vec<T>::t V;
   constexpr int NB = L / R;
   const int total = a.W * NB;
+  // the first pass (NS = 1) writes each butterfly's R outputs R apart:
+  // with lanes of a power-of-two count, consecutive threads take
+  // consecutive lanes instead (odd lane stride Lp: distinct banks)
+  const bool lf = NS == 1 && a.W >= 4 && (a.W & (a.W - 1)) == 0;
+  const int lgw = __ffs(a.W) - 1;
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
-    const int lane = i / NB, j = i - lane * NB, k = j % NS;
+    const int lane = lf ? (i & (a.W - 1)) : i / NB;
+    const int j = lf ? (i >> lgw) : i - lane * NB, k = j % NS;
     const V* s = src + lane * a.Lp;
     V v[R];
 #pragma unroll
