@@ -38,9 +38,14 @@ __device__ __forceinline__ void block_pass(const typename Vec<T>::t* __restrict_
   const bool wr_lin = (p.Ns & ((1 << (PS + 4)) - 1)) == 0;
   const int rd_st = nb + (nb >> PS) + (nb >> (PS + 4));
   const int wr_st = (int)p.Ns + ((int)p.Ns >> PS) + ((int)p.Ns >> (PS + 4));
+  // the first pass (Ns = 1) writes each butterfly's R outputs R apart: with
+  // lanes of a power-of-two count, consecutive threads take consecutive
+  // lanes instead (the odd lane stride Lp spreads them over the banks)
+  const bool lf = p.Ns == 1 && a.W >= 4 && (a.W & (a.W - 1)) == 0;
+  const int lgw = __ffs(a.W) - 1;
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
-    const int lane = (int)fdiv((unsigned)i, p.fd_nb);
-    const int j = i - lane * nb;
+    const int lane = lf ? (i & (a.W - 1)) : (int)fdiv((unsigned)i, p.fd_nb);
+    const int j = lf ? (i >> lgw) : i - lane * nb;
     const V* s = src + lane * a.Lp;
     V* d = dst + lane * a.Lp;
     V v[R];

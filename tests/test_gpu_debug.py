@@ -29,7 +29,8 @@ CHILD = textwrap.dedent("""
     cases = [(4096, 1, 0, 3, None), (1 << 16, 1, 0, 2, None), (1 << 20, 1, 0, 1, None), (1 << 13, 0, 0, 2, None),
              (1 << 19, 0, 2, 1, None), (1 << 19, 0, 3, 1, None), (1 << 14, 1, 2, 2, None), (3 * 2 ** 14, 1, 0, 2, None),
              (1000, 0, 0, 3, {"kernel_variant": 1}), (5 ** 6, 1, 0, 2, None), (1 << 16, 1, 0, 2, {"decimation": 1}),
-             (12288, 0, 1, 2, {"kernel_variant": 4})]
+             (12288, 0, 1, 2, {"kernel_variant": 4}), (3 * 2 ** 18, 1, 0, 1, None), (5 ** 8, 1, 1, 1, None),
+             (360 * 360, 1, 0, 1, None), (1 << 18, 1, 1, 2, {"blocks_per_sm": 2}), (8192, 1, 0, 3, None)]
     for n, vt, tr, b, opts in cases:
         dt = np.float64 if vt == 0 else np.float32
         x = inputs.gaussian(n + tr, 2 * n * b).astype(dt)
