@@ -102,6 +102,8 @@ template <typename T, int L, int RF, int TK = 64> struct Geo {
   static constexpr int HC = colshape::width_c(esz<T>(), RF);
   static constexpr int OFF_B = WA * L, OFF_C = (WA + HB) * L;  // elements
   static constexpr int TB = colshape::stage_bytes(esz<T>(), L, RF, TK);
+  static constexpr int FB = colshape::ftw_box_bytes(esz<T>(), L, RF, TK);  // four-step factor block
+  static constexpr int TS = TB + FB;                                      // stage stride
   static constexpr int WORK = colshape::work_bytes_rf(esz<T>(), L, RF, TK);
 };
 
@@ -349,7 +351,7 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
   typedef Shape<T, L, TK> Sh;
   typedef Geo<T, L, RF, TK> Gm;
   typedef typename Vec<T>::t V;
-  constexpr int W = Sh::W, NT = Sh::NT, NP = Sh::NP, TB = Gm::TB, BR = Sh::BR, NBOX = Sh::NBOX;
+  constexpr int W = Sh::W, NT = Sh::NT, NP = Sh::NP, TB = Gm::TB, TS = Gm::TS, BR = Sh::BR, NBOX = Sh::NBOX;
   constexpr int NB0 = L / radix_of(L, 0);  // first pass: radix 16, one butterfly per thread
   constexpr int NBL = L / radix_of(L, NP - 1), QL = 16 / radix_of(L, NP - 1);
   constexpr int RL = radix_of(L, NP - 1);
@@ -358,13 +360,13 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
   static_assert(NP > 1, "column tiles have two or more in-block passes");
   extern __shared__ __align__(1024) unsigned char smem[];
   const int S = a.stages;
-  V* const work = reinterpret_cast<V*>(smem + (size_t)S * TB);
+  V* const work = reinterpret_cast<V*>(smem + (size_t)S * TS);
   // the pass's in-block twiddles (L - 1 entries from pass[0].tw on),
   // copied once per block: shared-memory loads instead of scattered L1 ones
   constexpr int TWN = colshape::tw_entries(L);
-  V* const stw = reinterpret_cast<V*>(smem + (size_t)S * TB + Gm::WORK);
+  V* const stw = reinterpret_cast<V*>(smem + (size_t)S * TS + Gm::WORK);
   uint64_t* const bars =
-      reinterpret_cast<uint64_t*>(smem + (size_t)S * TB + Gm::WORK + colshape::tw_bytes(esz<T>(), L));
+      reinterpret_cast<uint64_t*>(smem + (size_t)S * TS + Gm::WORK + colshape::tw_bytes(esz<T>(), L));
   const int tw0 = a.pass[0].tw;
   for (int e = threadIdx.x; e < TWN; e += NT) stw[e] = __ldg((const V*)a.tw + tw0 + e);
   const V* tw = stw;
@@ -375,6 +377,7 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
   const long long stride = a.stride;  // N / L: units per transform
   const long long tpt = stride / W;   // tiles per transform
   const long long gNs = a.gNs;
+  const bool fbox = !RF && a.ftw_box && a.ftw && gNs > 1;  // factors staged with the tile
   const unsigned kfac = (unsigned)(a.N / (gNs * L));
   const V* lo = (const V*)a.gtw_lo;
   const V* hi = (const V*)a.gtw_hi;
@@ -391,12 +394,14 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
     const long long t = tile / tpt, p = tile - t * tpt;
     const int y = (int)(t * L);
     const uint32_t bar = fast::saddr(&bars[s]);
-    unsigned char* st = smem + (size_t)s * TB;
+    unsigned char* st = smem + (size_t)s * TS;
     if (!RF) {
-      fast::mbar_expect_tx(bar, (uint32_t)TB);
+      fast::mbar_expect_tx(bar, (uint32_t)(TB + (fbox ? Gm::FB : 0)));
 #pragma unroll 1
       for (int k = 0; k < NBOX; ++k)
         tma_load_2d(fast::saddr(st + (size_t)k * BR * W * esz<T>()), &maps.in[0], (int)(p * W * XS), y + k * BR, bar);
+      // the tile's units p W .. p W + W - 1 have k = (p W) mod Ns + lane
+      if (fbox) tma_load_2d(fast::saddr(st + TB), &maps.in[1], (int)(((p * W) % gNs) * XS), 0, bar);
     } else {
       const int wc = p == 0 ? Gm::HC : 0;
       fast::mbar_expect_tx(bar, (uint32_t)(NBOX * BR * (Gm::H + Gm::HB + wc) * esz<T>()));
@@ -441,7 +446,7 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
       return;
     }
     const long long t = tile / tpt, p = tile - t * tpt;
-    V* const st = reinterpret_cast<V*>(smem + (size_t)s * TB);
+    V* const st = reinterpret_cast<V*>(smem + (size_t)s * TS);
     if constexpr (RF == 2) {
       // real inverse: recover Z from the packed spectrum before the butterflies
       real_tile<T, L, RF, NT>(st, p, stride, a.N, rtw, a.status);
@@ -456,8 +461,10 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
       const V* sp = st + src.base + src.col;
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
-        const int e = src.base + src.col + (j + r * NB0) * src.width;
-        if (GFFT_DCHECK(e >= 0 && e < TB / (int)sizeof(V), a.status)) v[r] = sp[(j + r * NB0) * src.width];
+        if (GFFT_DCHECK(src.base + src.col + (j + r * NB0) * src.width >= 0 &&
+                            src.base + src.col + (j + r * NB0) * src.width < TB / (int)sizeof(V),
+                        a.status))
+          v[r] = sp[(j + r * NB0) * src.width];
       }
       if (conj)
 #pragma unroll
@@ -470,9 +477,16 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
           // the first factor per thread, the second from the [r][k] table
           const unsigned m0 = kstep * (unsigned)j;  // < N < 2^32
           const V t0 = cmul(__ldg(lo + (m0 & mask)), __ldg(hi + (m0 >> lgB)));
-          const V* t2 = (const V*)a.ftw + k;
+          if (fbox) {
+            // the tile's block of factors, staged with it: [r][lane]
+            const V* t2 = reinterpret_cast<const V*>(reinterpret_cast<const unsigned char*>(st) + TB) + lane;
 #pragma unroll
-          for (int r = 0; r < 16; ++r) v[r] = cmul(v[r], cmul(t0, __ldg(t2 + (size_t)r * gNs)));
+            for (int r = 0; r < 16; ++r) v[r] = cmul(v[r], cmul(t0, t2[r * W]));
+          } else {
+            const V* t2 = (const V*)a.ftw + k;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = cmul(v[r], cmul(t0, __ldg(t2 + (size_t)r * gNs)));
+          }
         } else if (kstep) {
 #pragma unroll
           for (int r = 0; r < 16; ++r) {
@@ -544,7 +558,7 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
 #pragma unroll 1
           for (int k = 0; k < NBOX; ++k)
             tma_store_2d(&maps.out[0], (int)(k0 * XS), (int)(row0 + k * BR),
-                         fast::saddr(smem + (size_t)S * TB + (size_t)k * BR * W * esz<T>()));
+                         fast::saddr(smem + (size_t)S * TS + (size_t)k * BR * W * esz<T>()));
           asm volatile("cp.async.bulk.commit_group;" ::: "memory");
         }
       } else {
@@ -552,7 +566,7 @@ __global__ void __launch_bounds__(col::Shape<T, L, TK>::NT, 64 / TK)
         // stores; region B by tensor stores where its box starts on a 16-byte
         // boundary (FP64) and lies inside the tensor (not the first tile, whose
         // box reaches column S), else, with region C, by plain stores
-        unsigned char* wb = smem + (size_t)S * TB;
+        unsigned char* wb = smem + (size_t)S * TS;
         const bool tb_b = Gm::F64 && p != 0;
         if (threadIdx.x == 0) {
 #pragma unroll 1

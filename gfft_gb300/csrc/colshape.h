@@ -46,6 +46,12 @@ constexpr int width_a(int esz, int L, int rf) { return rf ? half(esz, L) : lanes
 constexpr int stage_bytes(int esz, int L, int rf, int tk = 64) {
   return rf ? (width_a(esz, L, rf) + width_b(esz, L, rf) + width_c(esz, rf)) * L * esz : lanes(esz, L, tk) * L * esz;
 }
+// a complex tile of a later pass brings its [16][W] block of four-step
+// factors W_(16 Ns)^(k r) along (tensor copy into the stage, after the tile)
+constexpr int ftw_box_bytes(int esz, int L, int rf, int tk = 64) { return rf ? 0 : 16 * lanes(esz, L, tk) * esz; }
+constexpr int stage_stride(int esz, int L, int rf, int tk = 64) {
+  return stage_bytes(esz, L, rf, tk) + ftw_box_bytes(esz, L, rf, tk);
+}
 constexpr int work_bytes_rf(int esz, int L, int rf, int tk = 64) {
   return work_bytes(esz, L, tk) > round1k(stage_bytes(esz, L, rf, tk)) ? work_bytes(esz, L, tk)
                                                                      : round1k(stage_bytes(esz, L, rf, tk));
@@ -67,7 +73,7 @@ constexpr int tw_bytes(int esz, int L) { return ((tw_entries(L) * esz + 15) / 16
 // shared memory of a launch with `stages` stages: the stages, the work
 // buffer, the in-block twiddles and one mbarrier per stage
 constexpr long long smem_bytes(int esz, int L, int rf, int stages, int tk = 64) {
-  return (long long)stages * stage_bytes(esz, L, rf, tk) + work_bytes_rf(esz, L, rf, tk) + tw_bytes(esz, L) +
+  return (long long)stages * stage_stride(esz, L, rf, tk) + work_bytes_rf(esz, L, rf, tk) + tw_bytes(esz, L) +
          8LL * stages;
 }
 

@@ -121,15 +121,24 @@ extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, int tk, unsigned gr
   if ((((uintptr_t)a->in) | ((uintptr_t)a->out)) & 15) return (int)cudaErrorInvalidValue;
   if (a->stride % W || (a->gNs > 1 && a->gNs % W)) return (int)cudaErrorInvalidValue;
   gfft::col::ColMaps m;
+  EngineArgs a2 = *a;
+  a2.ftw_box = 0;
   const long long rows_in = batch * a->L, rows_out = batch * (a->N / a->gNs);
   if (!rf) {
     if (encode(&m.in[0], a->in, rows_in, a->stride, esz, W, br) != 0) return (int)cudaErrorInvalidValue;
+    m.in[1] = m.in[2] = m.in[0];
     if (a->gNs > 1) {
       if (encode(&m.out[0], a->out, rows_out, a->gNs, esz, W, br) != 0) return (int)cudaErrorInvalidValue;
+      // the [16][Ns] four-step factors, one [16][W] box per tile, where the
+      // table (16 Ns values) outgrows L1: measured at 2^28 points, 6-10 %
+      // faster for Ns >= 1024 (2^20 .. 2^24), about 1 % slower for Ns <= 512
+      // (else the kernel reads them from global memory)
+      if (a->ftw && a->gNs >= 1024 && !(((uintptr_t)a->ftw) & 15) &&
+          encode(&m.in[1], a->ftw, 16, a->gNs, esz, W, 16) == 0)
+        a2.ftw_box = 1;
     } else {
       m.out[0] = m.in[0];  // unused: the first pass stores from registers
     }
-    m.in[1] = m.in[2] = m.in[0];
     m.out[1] = m.out[2] = m.out[0];
   } else {
     // regions A (W/2 columns), B (the mirrors; FP32 two wider) and C (column S/2)
@@ -150,6 +159,6 @@ extern "C" int gfft_col_launch(int dbl, const EngineArgs* a, int tk, unsigned gr
     }
   }
   cudaGetLastError();  // clear a stale error of an earlier, unrelated call
-  void* args[] = {(void*)a, (void*)&m};
+  void* args[] = {(void*)&a2, (void*)&m};
   return (int)cudaLaunchKernel(f, dim3(grid), dim3(threads), args, smem, stream);
 }

@@ -101,6 +101,7 @@ struct EngineArgs {
   int notw;           // lane passes without the four-step twiddle (axis transforms of a multi-dimensional array)
   const void* ftw;    // variant 9, later global passes: W_(R0 Ns)^(k r) at [r * Ns + k] (null: two-level lookups)
   int dif;            // generic engine: frequency decimation (transposed passes, twiddles after the butterflies)
+  int ftw_box;        // variant 9: a tile's [16][W] block of ftw arrives with it by tensor copy (ColMaps in[1])
   BlockPass pass[GFFT_MAXP];
 };
 

@@ -590,6 +590,7 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   for (int g = 1; g < plan.nglobal; ++g) {
     const GlobalPass& gp = plan.gp[g];
     if (gp.variant == 9 && gp.pass[0].R * gp.Ns <= (1LL << 20)) {
+      off += off & 1;  // 16-byte aligned (FP32 complex: an even element offset) for tensor copies
       plan.ftw_off[g] = off;
       off += (std::size_t)(gp.pass[0].R * gp.Ns);
     }
