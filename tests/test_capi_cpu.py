@@ -287,3 +287,41 @@ def test_decimation_option():
         with pytest.raises(_lib.GfftError) as e:
             _lib.plan_query(64, 0, 0, 1, 1, bad)
         assert e.value.status == 14
+
+
+def test_mixed_column_tile_shapes():
+    """Shape arithmetic of the mixed-radix column tiles (host only): units per
+    tile (power of two, tile <= 64 KB), 512 threads, shared memory within one
+    SM for one stage; tensor copies need boxes starting on 128-byte
+    boundaries (729 = 9.9.9 and 625 = 5.5.5.5: odd row counts per box of
+    64-byte rows do not), gathers take any shape of the compiled list, at
+    most two stages."""
+    import ctypes
+    L = _lib.lib()
+    f = L.gfft_colmix_shape
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_size_t)]
+
+    def shape(dbl, n, rs, stages, gather):
+        arr = (ctypes.c_int * 4)(*(list(rs) + [1] * (4 - len(rs))))
+        w, t, sm = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+        st = f(dbl, n, arr, len(rs), stages, gather, ctypes.byref(w), ctypes.byref(t), ctypes.byref(sm))
+        return st, w.value, t.value, sm.value
+
+    for n, rs in ((768, (16, 16, 3)), (576, (16, 12, 3)), (432, (16, 9, 3)), (1000, (10, 10, 10)),
+                  (480, (16, 15, 2)), (360, (15, 12, 2))):
+        for dbl in (0, 1):
+            esz = 16 if dbl else 8
+            st, w, t, sm = shape(dbl, n, rs, 1, 0)
+            assert st == 0 and t == 512, (n, dbl)
+            assert w & (w - 1) == 0 and w * n * esz <= 65536 < 2 * w * n * esz, (n, dbl, w)
+            assert sm <= 227 * 1024, (n, dbl, sm)
+            assert shape(dbl, n, rs, 1, 1)[0] == 0
+    assert shape(0, 729, (9, 9, 9), 1, 0)[0] == 1   # no tensor copies
+    assert shape(0, 625, (5, 5, 5, 5), 1, 0)[0] == 1
+    assert shape(0, 625, (5, 5, 5, 5), 2, 1)[0] == 0
+    assert shape(0, 729, (9, 9, 9), 1, 1)[0] == 0   # gathers
+    assert shape(0, 729, (9, 9, 9), 3, 1)[0] == 1   # gathers: one or two stages
+    assert shape(0, 768, (16, 8, 6), 1, 0)[0] == 1  # not a compiled shape
+    assert shape(0, 1024, (16, 16, 4), 1, 0)[0] == 1  # powers of two are col.cuh's
