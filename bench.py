@@ -776,7 +776,8 @@ def main():
                     best = min(best, time.perf_counter() - t0)
             link[name + "_gbs"] = nel * 4 / best / 1e9
         del dx
-        obj.fft(hx, hy)  # allocates the staging buffer once
+        for _ in range(3):  # the first call allocates the staging buffer and the slice plans
+            obj.fft(hx, hy)
         e2e_steps = max(3, min(args.steps, 10))
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
