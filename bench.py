@@ -41,10 +41,10 @@ BATCH = 65536
 WORKLOAD = "fp32 c2c fft N=4096 x batch 65536, out of place"
 
 # DRAM bytes (read + write) of one launch on this workload: one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum of spec_kernel<float, 4096>)
-# measured 1.0265e9 bytes for batch 16384; traffic scales with the
-# transforms processed (x4).
-NCU_TRAFFIC_BYTES = {(4096, 65536): 4 * 1.0265e9}
+# (dram__bytes_read.sum + dram__bytes_write.sum of spec_direct_kernel<float,
+# 4096, 4>) measured 0.53696e9 + 0.48948e9 bytes for batch 16384; traffic
+# scales with the transforms processed (x4).
+NCU_TRAFFIC_BYTES = {(4096, 65536): 4 * 1.02644e9}
 
 
 def parse():

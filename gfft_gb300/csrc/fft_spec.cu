@@ -109,6 +109,44 @@ __global__ void __launch_bounds__(spec::tile_of<T>(L) / 16, 1) spec_kernel(const
 }
 
 
+// One transform per block with no stage (stages = 0): the whole transform in
+// the registers of L / 16 threads (16 values each); the first pass loads
+// straight from global memory (consecutive threads read consecutive
+// elements of each leg: coalesced), the middle passes go through the padded
+// work buffer and the last pass stores straight to global memory; the next
+// transform's loads are issued while other warps still finish the previous
+// one's last pass.  FP32 16384 (one block of 1024 threads per SM: a stage
+// and the work buffer would not both fit the shared memory), 8192 / 4096
+// with MINB = 2 / 4 blocks per SM (64 registers; the blocks of an SM hide
+// each other's load latency, no stage needed).
+template <typename T, int L, int MINB>
+__global__ void __launch_bounds__(L / 16, MINB) spec_direct_kernel(const __grid_constant__ EngineArgs a) {
+  using namespace spec;
+  typedef typename Vec<T>::t V;
+  static_assert(L >= Cfg<T>::TILE, "one transform per block");
+  constexpr int NP = npass_of(L);
+  static_assert(NP > 1, "two or more passes");
+  extern __shared__ __align__(128) unsigned char smem[];
+  V* work = reinterpret_cast<V*>(smem);
+  const V* in = (const V*)a.in;
+  V* out = (V*)a.out;
+  const V* tw = (const V*)a.tw;
+  const bool conj = a.conj != 0;
+  const T sc = (T)a.scale;
+  V v[16];
+  for (long long t = blockIdx.x; t < a.nunits; t += gridDim.x) {
+    sread<T, L, 0, true>(v, in + t * L);  // global loads, 16 in flight per thread
+    if (conj)
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = cconj(v[i]);
+    scompute<T, L, 0>(v, tw, a.pass[0].tw);
+    __syncthreads();  // the previous transform's last pass has read the work buffer
+    swrite<T, L, 0>(v, work);
+    __syncthreads();
+    rest<T, L, 1>(v, work, tw, a.pass, out + t * L, 1, conj, sc);
+  }
+}
+
 // ---- power-of-two column tiles of a multi-pass length (variant 5) --------
 // The passes of spec_kernel, for the W = tile / L adjacent lanes of a global
 // pass (plan.h): the next tile is gathered with 8/16-byte cp.async copies
@@ -238,9 +276,22 @@ const void* spec_fn(int L) {
 }
 }  // namespace
 
-// lengths with a specialised kernel: FP32 16..8192, FP64 16..2048
+namespace {
+// the stage-free one-transform-per-block kernels (FP32)
+const void* direct_fn(int dbl, int L) {
+  if (dbl) return nullptr;
+  switch (L) {
+    case 4096: return (const void*)gfft::spec_direct_kernel<float, 4096, 4>;
+    case 8192: return (const void*)gfft::spec_direct_kernel<float, 8192, 2>;
+    case 16384: return (const void*)gfft::spec_direct_kernel<float, 16384, 1>;
+    default: return nullptr;
+  }
+}
+}  // namespace
+
+// lengths with a specialised kernel: FP32 16..16384, FP64 16..2048
 extern "C" int gfft_spec_supported(int dbl, int L) {
-  return (dbl ? spec_fn<double>(L) : spec_fn<float>(L)) != nullptr;
+  return direct_fn(dbl, L) != nullptr || (dbl ? spec_fn<double>(L) : spec_fn<float>(L)) != nullptr;
 }
 
 extern "C" int gfft_spec_setup(int dbl, size_t max_smem) {
@@ -248,11 +299,15 @@ extern "C" int gfft_spec_setup(int dbl, size_t max_smem) {
   int e = spec_setup_all<float>(max_smem);
   e |= spec_setup_one<float, 4096>(max_smem);
   e |= spec_setup_one<float, 8192>(max_smem);
+  for (int L : {4096, 8192, 16384})
+    e |= cudaFuncSetAttribute(direct_fn(0, L), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem) !=
+         cudaSuccess;
   return e;
 }
 
-extern "C" int gfft_spec_occupancy(int dbl, int L, int threads, size_t smem) {
-  const void* f = dbl ? spec_fn<double>(L) : spec_fn<float>(L);
+
+extern "C" int gfft_spec_occupancy(int dbl, int L, int stages, int threads, size_t smem) {
+  const void* f = stages == 0 ? direct_fn(dbl, L) : (dbl ? spec_fn<double>(L) : spec_fn<float>(L));
   if (!f) return 0;
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem);
@@ -261,7 +316,7 @@ extern "C" int gfft_spec_occupancy(int dbl, int L, int threads, size_t smem) {
 
 extern "C" int gfft_spec_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                 cudaStream_t stream) {
-  const void* f = dbl ? spec_fn<double>(a->L) : spec_fn<float>(a->L);
+  const void* f = a->stages == 0 ? direct_fn(dbl, a->L) : (dbl ? spec_fn<double>(a->L) : spec_fn<float>(a->L));
   if (!f) return (int)cudaErrorInvalidValue;
   void* args[] = {(void*)a};
   return (int)cudaLaunchKernel(f, dim3(grid), dim3(threads), args, smem, stream);

@@ -29,7 +29,7 @@ extern "C" int gfft_fast_occupancy(int dbl, int threads, size_t smem);
 extern "C" int gfft_fast_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                 cudaStream_t stream);
 extern "C" int gfft_spec_setup(int dbl, size_t max_smem);
-extern "C" int gfft_spec_occupancy(int dbl, int L, int threads, size_t smem);
+extern "C" int gfft_spec_occupancy(int dbl, int L, int stages, int threads, size_t smem);
 extern "C" int gfft_spec_launch(int dbl, const EngineArgs* a, unsigned grid, unsigned threads, size_t smem,
                                 cudaStream_t stream);
 extern "C" int gfft_lane_setup(int dbl, size_t max_smem);
@@ -191,7 +191,7 @@ int gfft_create_opts(gfft_handle* handle, uint64_t n, int vtype_id, int trans_id
       if (gp.variant < 2) continue;
       int per = (opts && opts->blocks_per_sm)
                     ? opts->blocks_per_sm
-                    : (gp.variant == 3   ? gfft_spec_occupancy(dbl, gp.L, gp.threads, gp.smem)
+                    : (gp.variant == 3   ? gfft_spec_occupancy(dbl, gp.L, gp.stages, gp.threads, gp.smem)
                        : gp.variant == 4 ? gfft_lane_occupancy(dbl, gp.threads, gp.smem)
                        : gp.variant == 5 ? gfft_lanep2_occupancy(dbl, gp.L, gp.threads, gp.smem)
                        : gp.variant == 6 ? gfft_tc_occupancy(gp.L, gp.threads, gp.smem)

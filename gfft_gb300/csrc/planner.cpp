@@ -285,6 +285,14 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
   long long col_cap = 2048;
   if (o.max_pass_len > 0) col_cap = std::min<long long>(o.max_pass_len, col_max);
 
+  // FP32 16384 in one pass (fft_spec.cu spec_direct_kernel: one transform
+  // per 1024-thread block, loaded straight from global memory) with the
+  // default radices and kernels
+  const bool direct16k = !dbl && n == 16384 && trans < 2 && (o.variant == 0 || o.variant == 3) &&
+                         o.radix_order == 0 && o.max_radix == 16 && o.units == 0 && o.threads == 0 &&
+                         (o.max_pass_len == 0 || o.max_pass_len >= 16384) && o.max_single == 0 &&
+                         o.smem_budget == 0 && o.stages == 0 && o.bps == 0 && !o.dif;
+  if (direct16k) cap1 = 16384;
   std::vector<long long> Ls;
   if (n <= cap1) {
     Ls.push_back(n);
@@ -540,6 +548,23 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
       while (S > 1 && S * SPT * esz + W * padded(gp.L) * esz + 8 * S > 220 * 1024) --S;
       gp.stages = S;
       gp.smem = (size_t)(S * SPT * esz + ((W * padded(gp.L) * esz + 7) & ~7LL) + 8 * S);
+    }
+    // one transform per block, no stage (spec_direct_kernel): FP32 4096 /
+    // 8192 / 16384 with 4 / 2 / 1 blocks per SM by default (measured at 2^28
+    // points: 86.4 -> 90.6 %, 68.0 -> 71.4 % of the copy bandwidth against
+    // the staged single pass; 47.2 -> 57.1 % against two passes); an
+    // explicit stage count keeps the staged kernel
+    const bool direct_req = !dbl && trans < 2 && plan.nglobal == 1 && (o.variant == 0 || o.variant == 3) &&
+                            o.radix_order == 0 && o.max_radix == 16 && o.units == 0 && o.threads == 0 &&
+                            o.stages == 0 && o.bps == 0 && (gp.L == 4096 || gp.L == 8192);
+    if (((direct16k && plan.nglobal == 1 && gp.L == 16384) || direct_req) && spec_radices(gp)) {
+      gp.variant = 3;
+      gp.units = 1;
+      gp.threads = gp.L / 16;
+      gp.stages = 0;
+      gp.tile_bytes = (int)(gp.L * esz);
+      gp.ntiles = batch;
+      gp.smem = (size_t)(padded(gp.L) * esz);  // the work buffer only
     }
     Ns *= gp.L;
   }

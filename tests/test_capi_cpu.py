@@ -69,12 +69,18 @@ def test_plan_shapes(n, vt, passes):
 def test_plan_power_of_two_uses_radix16():
     d = _lib.plan_query(4096, 1, 0, 1, 65536)
     assert d["radices"] == [[16, 16, 16]]
-    # FP32 8192: the length-specialised single pass, one transform per tile,
-    # 512 threads, two stages; variant 2 on request
+    # FP32 8192: the length-specialised single pass, one transform per
+    # block, 512 threads; variant 2 on request
     d = _lib.plan_query(8192, 1, 0, 1, 100)
     assert d["kernel_variant"] == [3] and d["threads"] == [512] and d["units"] == [1], d
     assert d["radices"] == [[16, 16, 8, 4]]
     assert _lib.plan_query(8192, 1, 0, 1, 100, {"kernel_variant": 2})["kernel_variant"] == [2]
+    # FP32 16384: one pass of 1024 threads, straight from global memory; two
+    # column-tile passes with any tuning option
+    d = _lib.plan_query(16384, 1, 0, 1, 100)
+    assert d["kernel_variant"] == [3] and d["threads"] == [1024] and d["radices"] == [[16, 16, 16, 4]], d
+    assert _lib.plan_query(16384, 1, 0, 1, 100, {"stages": 1})["kernel_variant"] == [9, 9]
+    assert _lib.plan_query(16384, 0, 0, 1, 100)["kernel_variant"] == [9, 9]
     d = _lib.plan_query(4096, 1, 0, 1, 1, {"max_radix": 4})
     assert d["radices"] == [[4] * 6]
 

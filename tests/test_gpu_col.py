@@ -120,7 +120,7 @@ def test_col_unaligned_buffers(cuda, n):
     assert np.array_equal(b, b2)
 
 
-@pytest.mark.parametrize("n,B", [(1 << 14, 3), (1 << 16, 2), (1 << 17, 2), (1 << 18, 2), (1 << 19, 1),
+@pytest.mark.parametrize("n,B", [(1 << 15, 3), (1 << 16, 2), (1 << 17, 2), (1 << 18, 2), (1 << 19, 1),
                                  (1 << 23, 1)])
 def test_col_half_tiles(cuda, oracle, n, B):
     """FP32 passes of 128 .. 512 run 32 KB tiles by default (half the units

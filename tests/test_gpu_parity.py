@@ -385,11 +385,31 @@ def test_c3_fp32_2pow24(cuda, oracle):
     assert abs(np.sum(yn.astype(np.float64) ** 2) / e_in - 1) <= 10 * tol(n, 0)
 
 
+@pytest.mark.parametrize("n,B", [(4096, 9), (8192, 5), (16384, 3)])
+def test_direct_single_pass(cuda, oracle, n, B):
+    """One transform per block with no stage (FP32 4096 / 8192 / 16384, the
+    defaults): against the exact oracle and the staged single pass (or the
+    two-pass plan at 16384), forward and inverse, in and out of place."""
+    from gfft_gb300 import _lib
+    opts = None
+    d = _lib.plan_query(n, 1, 0, 1, B, opts)
+    assert d["kernel_variant"] == [3] and d["threads"] == [n // 16], d
+    x = inputs.gaussian(61 + n, 2 * n * B).astype(np.float32)
+    for tr in (0, 1):
+        y = run_gpu(cuda, n, 1, tr, 1, x, batch=B, opts=opts)
+        ex = oracle.fft_ld(x.astype(np.float64), n, B, 1 if tr == 0 else -1)
+        assert rel(y, ex) <= tol(n, 0), (n, tr, rel(y, ex))
+        ref = run_gpu(cuda, n, 1, tr, 1, x, batch=B, opts={"stages": 1})
+        assert rel(y, ref) <= tol(n, 0), (n, tr, rel(y, ref))
+        yi = run_gpu(cuda, n, 1, tr, 0, x, batch=B, opts=opts)
+        assert np.array_equal(y, yi), (n, tr)
+
+
 def test_fast_path_matches_generic_engine(cuda, oracle):
     """The pipelined register-resident kernel (variant 2) against the generic
     engine (variant 1) and the exact oracle, single and partial tiles."""
     for n, dbl, B in ((4096, 0, 7), (1024, 1, 9), (16, 0, 1000), (64, 0, 300), (8192, 0, 3), (2048, 1, 5),
-                      (256, 1, 33)):
+                      (256, 1, 33), (16384, 0, 5)):
         dt = np.float64 if dbl else np.float32
         vt = 0 if dbl else 1
         x = inputs.uniform(55 + n, 2 * n * B).astype(dt)
