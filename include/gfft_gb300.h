@@ -97,7 +97,10 @@ typedef struct gfft_plan_opts {
                              9 = column tiles moved by 2-D tensor copies (passes of 64..4096
                                  of a multi-pass power-of-two length; device buffers
                                  16-byte aligned, others run through variant 5) */
-  int stages;             /* bulk-copy pipeline depth of the fast path (0 = 2) */
+  int stages;             /* bulk-copy pipeline depth of the pipelined kernels (0 = the planner's
+                             choice; FP32 single passes of 4096 / 8192 / 16384 then load straight
+                             from global memory, one transform per block, and any explicit depth
+                             selects the staged kernel instead) */
   int blocks_per_sm;      /* persistent blocks per SM of the fast path (0 = occupancy); for the
                              tensor-copy column tiles, 1 keeps 64 KB tiles on FP32 passes of
                              128..512 (default there: 32 KB tiles, one stage, two blocks per SM)
