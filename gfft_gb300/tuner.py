@@ -204,7 +204,9 @@ def default_model():
 
 def choose(model, n, vtype=1, trans=0, place=1, batch=1, k=1, reps=5):
     """Plan options for (n, ...): the model's first choice (k=1), the best
-    measured of its top k, or the exhaustive measured best (model=None)."""
+    measured of its top k and the planner's default plan (so the measured
+    choice is never slower than the default), or the exhaustive measured best
+    (model=None)."""
     cands = candidates(n, vtype, trans, place, batch)
     if model is None:
         ms = measure(n, vtype, trans, place, batch, cands, reps)
@@ -216,6 +218,8 @@ def choose(model, n, vtype=1, trans=0, place=1, batch=1, k=1, reps=5):
     if len(order) == 1:
         return cands[int(order[0])], float(pred[order[0]])
     sub = [cands[int(i)] for i in order]
+    if {} in cands and {} not in sub:
+        sub.append({})
     ms = measure(n, vtype, trans, place, batch, sub, reps)
     ok = np.where(ms > 0, ms, np.inf)
     return sub[int(np.argmin(ok))], float(np.min(ok))

@@ -46,7 +46,7 @@ def run(torch, n, vt, tr, pl, x, batch=1, opts=None, offset=0):
     return r
 
 
-CASES = [(1 << 13, 1, 2), (1 << 14, 0, 5), (1 << 15, 0, 3), (1 << 16, 0, 2), (1 << 17, 0, 2),
+CASES = [(1 << 13, 1, 2), (1 << 14, 1, 5), (1 << 15, 0, 3), (1 << 16, 0, 2), (1 << 17, 0, 2),
          (1 << 18, 0, 2), (1 << 19, 0, 1), (1 << 20, 0, 2), (1 << 21, 0, 1), (1 << 22, 0, 1), (1 << 16, 1, 3),
          (1 << 19, 1, 1), (1 << 20, 1, 1), (1 << 22, 1, 1)]
 
