@@ -630,6 +630,11 @@ int gfft_plan_build(HostPlan& plan, long long n, long long batch, int dbl, int t
 }
 
 void gfft_plan_tables(const HostPlan& plan, double* tab) {
+  // alignment gaps between the tables hold 1 (never read; every entry a root of unity)
+  for (std::size_t i = 0; i < plan.table_count; ++i) {
+    tab[2 * i] = 1.0;
+    tab[2 * i + 1] = 0.0;
+  }
   for (int g = 0; g < plan.nglobal; ++g) {
     const GlobalPass& gp = plan.gp[g];
     for (int i = 0; i < gp.npass; ++i) {

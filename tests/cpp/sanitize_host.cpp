@@ -65,8 +65,9 @@ int main() {
   // the planner and the host side of the C ABI
   std::vector<uint64_t> lens;
   for (uint64_t n = 1; n <= 1100; ++n) lens.push_back(n);
-  for (uint64_t n : {2048ull, 3000ull, 4096ull, 4099ull, 8192ull, 12288ull, 15625ull, 65536ull, 248832ull, 390625ull,
-                     524288ull, 786432ull, 1ull << 20, 1ull << 22, 1ull << 24, 1ull << 27, 2ull * 4099})
+  for (uint64_t n : {2048ull, 3000ull, 4096ull, 4099ull, 8192ull, 12288ull, 15625ull, 16384ull, 65536ull, 129600ull,
+                     230400ull, 248832ull, 390625ull, 524288ull, 531441ull, 786432ull, 1000000ull, 1ull << 20,
+                     1ull << 22, 1ull << 24, 1ull << 27, 2ull * 4099})
     lens.push_back(n);
   const int variants[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9};
   for (uint64_t n : lens)
@@ -83,6 +84,13 @@ int main() {
               o.radix_order = (int)(n % 3);
               o.decimation = (v == 1 || v == 0) && (n % 2) ? 1 : 0;
               check_plan(n, vt, tr, pl, 4, &o);
+              // tile-size and stage options of the column tiles and the single pass
+              o.decimation = 0;
+              o.max_pass_len = 0;
+              o.radix_order = 0;
+              o.blocks_per_sm = 1 + (int)(n % 2);
+              o.stages = (int)(n % 3);
+              check_plan(n, vt, tr, pl, 3, &o);
             }
           }
         }
@@ -93,7 +101,7 @@ int main() {
   CHECK(gfft_plan_query(16, 0, 0, 1, 1, nullptr, nullptr) == GFFT_E_NULL_POINTER, "null info");
   for (int s = -2; s < 20; ++s) CHECK(gfft_strerror(s) != nullptr, "strerror %d", s);
   // every table entry a root of unity
-  for (uint64_t n : {2ull, 60ull, 1000ull, 4096ull, 8192ull, 786432ull, 1ull << 20})
+  for (uint64_t n : {2ull, 60ull, 1000ull, 4096ull, 8192ull, 16384ull, 390625ull, 786432ull, 1ull << 20, 1ull << 24})
     for (int dbl = 0; dbl < 2; ++dbl)
       for (int tr : {0, 2}) {
         PlanOpts po;
