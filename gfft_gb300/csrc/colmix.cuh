@@ -24,7 +24,9 @@
 //    tile's first write waits for (cp.async.bulk.wait_group.read).
 // Requirements (planner): W divides N / L and Ns (so a tile lies in one
 // transform and maps to one output box), row pitches of a multiple of 16
-// bytes, 16-byte aligned buffers.
+// bytes, 16-byte aligned buffers, tensor boxes starting on 128-byte
+// boundaries of the stage.  colmix_gather_kernel (below) has the same passes
+// with per-element cp.async gathers for the passes that miss these.
 //
 // Replaces, for mixed radices, the same recursion levels as col.cuh:
 // InTimeOOP (src/gfftalg.h:459-507) with DFTk_x_Im_T (src/gfftalg.h:169-267).
